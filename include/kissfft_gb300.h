@@ -1,0 +1,91 @@
+/*
+ * kissfft_gb300 core C API -- GPU KISS FFT plans with the sample type as a
+ * run-time tag.
+ *
+ * This is the layer under the per-type drop-in libraries (kiss_fft_cuda.h):
+ * it exposes batched execution, explicit streams and the fast FIR.  Every
+ * function here has a counterpart in the reference (mborgerding/kissfft):
+ *
+ *   kfg_plan_c2c   kiss_fft_alloc      (kiss_fft.h:117,   kiss_fft.c:337-372)
+ *   kfg_plan_real  kiss_fftr_alloc     (kiss_fftr.h:29,   kiss_fftr.c:21-61)
+ *   kfg_plan_nd    kiss_fftnd_alloc    (kiss_fftnd.h:20,  kiss_fftnd.c:20-92)
+ *   kfg_plan_ndr   kiss_fftndr_alloc   (kiss_fftndr.h:23, kiss_fftndr.c:30-84)
+ *   kfg_plan_fir   kiss_fastfir_alloc  (tools/kiss_fastfir.c:59-165, REAL_FASTFIR)
+ *   kfg_exec       kiss_fft / kiss_fftr / kiss_fftri / kiss_fftnd / kiss_fftndr /
+ *                  kiss_fftndri        (one transform per call)
+ *   kfg_exec_stride kiss_fft_stride    (kiss_fft.h:134)
+ *   kfg_exec_batch  a loop of the above over `batch` transforms, in one launch
+ *   kfg_fir_filter  kiss_fastfir over a whole signal plus its flush call
+ *                  (tools/kiss_fastfir.c:222-239)
+ *   kfg_next_fast_size kiss_fft_next_fast_size (kiss_fft.h:150)
+ *
+ * Data layout is the reference's: interleaved {r, i} pairs of the sample
+ * type (kiss_fft.h:87-90); real transforms take n reals and give n/2+1
+ * bins; N-D arrays are row-major; N-D-real halves the last axis.
+ * Normalisation is the reference's: none for float/double, 1/N per
+ * direction for Q15/Q31 (fixed-point outputs are bit-identical to the
+ * reference's fixed-point builds).
+ *
+ * Pointers may be device pointers (the fast path: the call is enqueued on
+ * the stream and returns) or host pointers (staged through device memory;
+ * the call returns when the result is in host memory).  There is no CPU
+ * fallback: without a usable GPU every call fails with KFG_ECUDA.
+ */
+#ifndef KISSFFT_GB300_H
+#define KISSFFT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KFG_FLOAT 0  /* kiss_fft_scalar = float   */
+#define KFG_DOUBLE 1 /* kiss_fft_scalar = double  */
+#define KFG_INT16 2  /* FIXED_POINT=16 (Q15)      */
+#define KFG_INT32 3  /* FIXED_POINT=32 (Q31)      */
+
+#define KFG_OK 0
+#define KFG_EINVAL (-1)       /* bad argument or unsupported size           */
+#define KFG_ENOMEM (-2)       /* device or host allocation failed           */
+#define KFG_ECUDA (-3)        /* a CUDA call failed (no GPU, launch error)  */
+#define KFG_EUNSUPPORTED (-4) /* valid in the reference, not built here      */
+
+typedef struct kfg_plan kfg_plan;
+
+kfg_plan *kfg_plan_c2c(int dtype, int nfft, int inverse);
+kfg_plan *kfg_plan_real(int dtype, int nfft, int inverse);
+kfg_plan *kfg_plan_nd(int dtype, const int *dims, int ndims, int inverse);
+kfg_plan *kfg_plan_ndr(int dtype, const int *dims, int ndims, int inverse);
+/* Real fast FIR (float).  taps: host array of ntaps floats.  nfft = 0 picks
+ * the reference's block size (next power of two above 2*(ntaps-1), at least
+ * 2048); the chosen size is returned through *nfft_out when non-null. */
+kfg_plan *kfg_plan_fir(const float *taps, size_t ntaps, size_t nfft, size_t *nfft_out);
+void kfg_plan_free(kfg_plan *p);
+
+/* stream: a cudaStream_t, or NULL for the library's current stream. */
+int kfg_exec(kfg_plan *p, const void *in, void *out, void *stream);
+int kfg_exec_stride(kfg_plan *p, const void *in, void *out, int in_stride, void *stream);
+/* in_dist / out_dist: element distance between consecutive transforms of the
+ * batch (complex elements or real samples, as the side holds); 0 = packed. */
+int kfg_exec_batch(kfg_plan *p, const void *in, void *out, long long batch, long long in_dist, long long out_dist,
+                   void *stream);
+/* Whole-signal filter: y receives nx - ntaps + 1 samples (the valid
+ * convolution); *ny_out gets that count. */
+int kfg_fir_filter(kfg_plan *p, const float *x, size_t nx, float *y, size_t *ny_out, void *stream);
+
+int kfg_set_stream(void *stream);
+void *kfg_get_stream(void);
+int kfg_synchronize(void);
+const char *kfg_last_error(void);
+int kfg_next_fast_size(int n);
+
+/* Plan introspection for tests and tools: out[0] = transform kind, out[1] =
+ * dtype, out[2] = length, out[3] = number of HBM passes of a 1-D plan,
+ * out[4] = kernel family, out[5] = tile length. */
+int kfg_plan_info(const kfg_plan *p, int *out, int nout);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,356 @@
+"""kissfft_gb300 -- KISS FFT on NVIDIA GB300 (sm_103a), driven through its C ABI.
+
+The functions of this module carry the reference's names and argument
+meaning (mborgerding/kissfft: kiss_fft.h, kiss_fftr.h, kiss_fftnd.h,
+kiss_fftndr.h, tools/kiss_fastfir.c) and call the drop-in libraries
+``libkissfft_cuda-<type>.so`` (include/kiss_fft_cuda.h) through ctypes::
+
+    import kissfft_gb300 as kf
+    cfg = kf.kiss_fft_alloc(1024, 0, dtype="float")
+    kf.kiss_fft(cfg, fin, fout)
+
+Buffers are numpy arrays (host memory: the call stages them and returns
+when done) or torch tensors on the GPU (the call is enqueued on torch's
+current stream).  Complex buffers use the reference layout: complex64 /
+complex128 for float / double, ``(..., 2)`` int16 / int32 arrays for Q15 /
+Q31.  As in the reference an alloc that fails returns None; a transform
+that fails prints the reference-style message on stderr and, here, also
+raises ``KissFFTError``.
+
+There is no CPU fallback: without the built libraries and a GPU every call
+fails loudly.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+DTYPES = ("float", "double", "int16_t", "int32_t")
+DTYPE_CODE = {"float": 0, "double": 1, "int16_t": 2, "int32_t": 3}
+_SCALAR_NP = {"float": "float32", "double": "float64", "int16_t": "int16", "int32_t": "int32"}
+
+_libs = {}
+_core = None
+
+
+class KissFFTError(RuntimeError):
+    pass
+
+
+def lib_dir():
+    return _build.LIB
+
+
+def _check_built():
+    if not os.path.exists(_build.core_lib()):
+        raise KissFFTError("kissfft_gb300 is not built: run `python -m kissfft_gb300.build` "
+                           "(no CPU fallback exists)")
+
+
+def core():
+    """The core library (include/kissfft_gb300.h)."""
+    global _core
+    if _core is None:
+        _check_built()
+        L = ctypes.CDLL(_build.core_lib(), mode=ctypes.RTLD_GLOBAL)
+        vp, i, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+        for fn in ("kfg_plan_c2c", "kfg_plan_real"):
+            getattr(L, fn).restype = vp
+            getattr(L, fn).argtypes = [i, i, i]
+        for fn in ("kfg_plan_nd", "kfg_plan_ndr"):
+            getattr(L, fn).restype = vp
+            getattr(L, fn).argtypes = [i, vp, i, i]
+        L.kfg_plan_fir.restype = vp
+        L.kfg_plan_fir.argtypes = [vp, ctypes.c_size_t, ctypes.c_size_t, vp]
+        L.kfg_plan_free.argtypes = [vp]
+        L.kfg_exec.argtypes = [vp, vp, vp, vp]
+        L.kfg_exec_stride.argtypes = [vp, vp, vp, i, vp]
+        L.kfg_exec_batch.argtypes = [vp, vp, vp, ll, ll, ll, vp]
+        L.kfg_fir_filter.argtypes = [vp, vp, ctypes.c_size_t, vp, vp, vp]
+        L.kfg_set_stream.argtypes = [vp]
+        L.kfg_get_stream.restype = vp
+        L.kfg_last_error.restype = ctypes.c_char_p
+        L.kfg_plan_info.argtypes = [vp, vp, i]
+        _core = L
+    return _core
+
+
+def load(dtype="float"):
+    """The drop-in library of one sample type (include/kiss_fft_cuda.h)."""
+    if dtype not in DTYPE_CODE:
+        raise ValueError("dtype must be one of %s" % (DTYPES,))
+    if dtype not in _libs:
+        core()
+        L = ctypes.CDLL(_build.dropin_lib(dtype))
+        vp, i, ll, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_size_t
+        for fn in ("kiss_fft_cuda_alloc", "kiss_fftr_cuda_alloc"):
+            getattr(L, fn).restype = vp
+            getattr(L, fn).argtypes = [i, i, vp, vp]
+        for fn in ("kiss_fftnd_cuda_alloc", "kiss_fftndr_cuda_alloc"):
+            getattr(L, fn).restype = vp
+            getattr(L, fn).argtypes = [vp, i, i, vp, vp]
+        L.kiss_fastfir_cuda_alloc.restype = vp
+        L.kiss_fastfir_cuda_alloc.argtypes = [vp, sz, vp, vp, vp]
+        for fn in ("kiss_fft_cuda", "kiss_fftr_cuda", "kiss_fftri_cuda", "kiss_fftnd_cuda", "kiss_fftndr_cuda",
+                   "kiss_fftndri_cuda"):
+            getattr(L, fn).argtypes = [vp, vp, vp]
+        L.kiss_fft_cuda_stride.argtypes = [vp, vp, vp, i]
+        for fn in ("kiss_fft_cuda_batch", "kiss_fftr_cuda_batch", "kiss_fftri_cuda_batch"):
+            getattr(L, fn).argtypes = [vp, vp, vp, ll, ll, ll]
+        for fn in ("kiss_fft_cuda_free", "kiss_fftr_cuda_free", "kiss_fftnd_cuda_free", "kiss_fftndr_cuda_free",
+                   "kiss_fastfir_cuda_free"):
+            getattr(L, fn).argtypes = [vp]
+        L.kiss_fastfir_cuda.restype = sz
+        L.kiss_fastfir_cuda.argtypes = [vp, vp, vp, sz, vp]
+        L.kiss_fastfir_cuda_filter.restype = sz
+        L.kiss_fastfir_cuda_filter.argtypes = [vp, vp, sz, vp]
+        L.kiss_fft_cuda_set_stream.argtypes = [vp]
+        L.kiss_fft_cuda_last_error.restype = ctypes.c_char_p
+        _libs[dtype] = L
+    return _libs[dtype]
+
+
+# ---------------------------------------------------------------- buffers
+def _ptr(buf):
+    """(pointer, is_torch_cuda) for a numpy array, a torch tensor or an int."""
+    if buf is None:
+        return None, False
+    if isinstance(buf, int):
+        return buf, False
+    if hasattr(buf, "data_ptr"):
+        if not buf.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return buf.data_ptr(), bool(buf.is_cuda)
+    if hasattr(buf, "ctypes"):
+        if not buf.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return buf.ctypes.data, False
+    raise TypeError("unsupported buffer type %r" % type(buf))
+
+
+def _use_torch_stream(L, *bufs):
+    for b in bufs:
+        if hasattr(b, "is_cuda") and b.is_cuda:
+            import torch
+            L.kiss_fft_cuda_set_stream(ctypes.c_void_p(torch.cuda.current_stream(b.device).cuda_stream))
+            return
+
+
+def _raise_on_status(L, where):
+    rc = L.kiss_fft_cuda_status()
+    if rc != 0:
+        msg = L.kiss_fft_cuda_last_error()
+        raise KissFFTError("%s failed (%d): %s" % (where, rc, msg.decode() if msg else ""))
+
+
+class Cfg(object):
+    """A drop-in cfg: the pointer returned by a kiss_*_cuda_alloc call.
+
+    Released by ``free()`` or when garbage-collected (the reference frees
+    with free(); a GPU cfg must go through kiss_*_cuda_free)."""
+
+    def __init__(self, lib, ptr, kind, dtype, **meta):
+        self.lib, self.ptr, self.kind, self.dtype = lib, ptr, kind, dtype
+        self.__dict__.update(meta)
+
+    def free(self):
+        if self.ptr:
+            self.lib.kiss_fft_cuda_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _mk(L, ptr, kind, dtype, **meta):
+    return Cfg(L, ptr, kind, dtype, **meta) if ptr else None
+
+
+# ---------------------------------------------------------------- kiss_fft.h
+def kiss_fft_alloc(nfft, inverse_fft=0, dtype="float"):
+    """kiss_fft_alloc (reference kiss_fft.h:117)."""
+    L = load(dtype)
+    return _mk(L, L.kiss_fft_cuda_alloc(int(nfft), int(inverse_fft), None, None), "c2c", dtype, nfft=int(nfft),
+               inverse=int(inverse_fft))
+
+
+def kiss_fft(cfg, fin, fout):
+    """kiss_fft (reference kiss_fft.h:129)."""
+    kiss_fft_stride(cfg, fin, fout, 1)
+
+
+def kiss_fft_stride(cfg, fin, fout, fin_stride):
+    """kiss_fft_stride (reference kiss_fft.h:134)."""
+    L = cfg.lib
+    _use_torch_stream(L, fin, fout)
+    L.kiss_fft_cuda_stride(ctypes.c_void_p(cfg.ptr), _ptr(fin)[0], _ptr(fout)[0], int(fin_stride))
+    _raise_on_status(L, "kiss_fft_stride")
+
+
+def kiss_fft_batch(cfg, fin, fout, batch, in_dist=0, out_dist=0):
+    """A batch of kiss_fft calls in one launch (distances in complex elements)."""
+    L = cfg.lib
+    _use_torch_stream(L, fin, fout)
+    rc = L.kiss_fft_cuda_batch(ctypes.c_void_p(cfg.ptr), _ptr(fin)[0], _ptr(fout)[0], int(batch), int(in_dist),
+                               int(out_dist))
+    if rc:
+        _raise_on_status(L, "kiss_fft_batch")
+
+
+def kiss_fft_free(cfg):
+    cfg.free()
+
+
+def kiss_fft_cleanup():
+    pass
+
+
+def kiss_fft_next_fast_size(n):
+    """kiss_fft_next_fast_size (reference kiss_fft.h:150)."""
+    return int(core().kfg_next_fast_size(int(n)))
+
+
+def kiss_fftr_next_fast_size_real(n):
+    """kiss_fftr_next_fast_size_real (reference kiss_fft.h:153-154)."""
+    return kiss_fft_next_fast_size((int(n) + 1) >> 1) << 1
+
+
+# ---------------------------------------------------------------- kiss_fftr.h
+def kiss_fftr_alloc(nfft, inverse_fft=0, dtype="float"):
+    """kiss_fftr_alloc (reference kiss_fftr.h:29); None for odd nfft."""
+    L = load(dtype)
+    return _mk(L, L.kiss_fftr_cuda_alloc(int(nfft), int(inverse_fft), None, None), "real", dtype, nfft=int(nfft),
+               inverse=int(inverse_fft))
+
+
+def kiss_fftr(cfg, timedata, freqdata):
+    """kiss_fftr (reference kiss_fftr.h:37)."""
+    L = cfg.lib
+    _use_torch_stream(L, timedata, freqdata)
+    L.kiss_fftr_cuda(ctypes.c_void_p(cfg.ptr), _ptr(timedata)[0], _ptr(freqdata)[0])
+    _raise_on_status(L, "kiss_fftr")
+
+
+def kiss_fftri(cfg, freqdata, timedata):
+    """kiss_fftri (reference kiss_fftr.h:43)."""
+    L = cfg.lib
+    _use_torch_stream(L, timedata, freqdata)
+    L.kiss_fftri_cuda(ctypes.c_void_p(cfg.ptr), _ptr(freqdata)[0], _ptr(timedata)[0])
+    _raise_on_status(L, "kiss_fftri")
+
+
+def kiss_fftr_batch(cfg, timedata, freqdata, batch, in_dist=0, out_dist=0):
+    L = cfg.lib
+    _use_torch_stream(L, timedata, freqdata)
+    rc = L.kiss_fftr_cuda_batch(ctypes.c_void_p(cfg.ptr), _ptr(timedata)[0], _ptr(freqdata)[0], int(batch),
+                                int(in_dist), int(out_dist))
+    if rc:
+        _raise_on_status(L, "kiss_fftr_batch")
+
+
+def kiss_fftri_batch(cfg, freqdata, timedata, batch, in_dist=0, out_dist=0):
+    L = cfg.lib
+    _use_torch_stream(L, timedata, freqdata)
+    rc = L.kiss_fftri_cuda_batch(ctypes.c_void_p(cfg.ptr), _ptr(freqdata)[0], _ptr(timedata)[0], int(batch),
+                                 int(in_dist), int(out_dist))
+    if rc:
+        _raise_on_status(L, "kiss_fftri_batch")
+
+
+# ---------------------------------------------------------------- kiss_fftnd.h / kiss_fftndr.h
+def kiss_fftnd_alloc(dims, inverse_fft=0, dtype="float"):
+    """kiss_fftnd_alloc (reference kiss_fftnd.h:20)."""
+    L = load(dtype)
+    d = (ctypes.c_int * len(dims))(*[int(x) for x in dims])
+    return _mk(L, L.kiss_fftnd_cuda_alloc(d, len(dims), int(inverse_fft), None, None), "nd", dtype, dims=list(dims),
+               inverse=int(inverse_fft))
+
+
+def kiss_fftnd(cfg, fin, fout):
+    """kiss_fftnd (reference kiss_fftnd.h:21)."""
+    L = cfg.lib
+    _use_torch_stream(L, fin, fout)
+    L.kiss_fftnd_cuda(ctypes.c_void_p(cfg.ptr), _ptr(fin)[0], _ptr(fout)[0])
+    _raise_on_status(L, "kiss_fftnd")
+
+
+def kiss_fftndr_alloc(dims, inverse_fft=0, dtype="float"):
+    """kiss_fftndr_alloc (reference kiss_fftndr.h:23); the last axis is the real one."""
+    L = load(dtype)
+    d = (ctypes.c_int * len(dims))(*[int(x) for x in dims])
+    return _mk(L, L.kiss_fftndr_cuda_alloc(d, len(dims), int(inverse_fft), None, None), "ndr", dtype,
+               dims=list(dims), inverse=int(inverse_fft))
+
+
+def kiss_fftndr(cfg, timedata, freqdata):
+    """kiss_fftndr (reference kiss_fftndr.h:31)."""
+    L = cfg.lib
+    _use_torch_stream(L, timedata, freqdata)
+    L.kiss_fftndr_cuda(ctypes.c_void_p(cfg.ptr), _ptr(timedata)[0], _ptr(freqdata)[0])
+    _raise_on_status(L, "kiss_fftndr")
+
+
+def kiss_fftndri(cfg, freqdata, timedata):
+    """kiss_fftndri (reference kiss_fftndr.h:40)."""
+    L = cfg.lib
+    _use_torch_stream(L, timedata, freqdata)
+    L.kiss_fftndri_cuda(ctypes.c_void_p(cfg.ptr), _ptr(freqdata)[0], _ptr(timedata)[0])
+    _raise_on_status(L, "kiss_fftndri")
+
+
+# ---------------------------------------------------------------- tools/kiss_fastfir.c
+def kiss_fastfir_alloc(imp_resp, nfft=0):
+    """kiss_fastfir_alloc (reference tools/kiss_fastfir.c:36, REAL_FASTFIR, float).
+
+    imp_resp: host float32 array of taps.  Returns the cfg (its ``nfft``
+    attribute holds the chosen block size) or None."""
+    import numpy as np
+    L = load("float")
+    h = np.ascontiguousarray(imp_resp, dtype=np.float32)
+    n = ctypes.c_size_t(int(nfft))
+    p = L.kiss_fastfir_cuda_alloc(h.ctypes.data, h.size, ctypes.byref(n), None, None)
+    return _mk(L, p, "fir", "float", nfft=int(n.value), ntaps=int(h.size))
+
+
+def kiss_fastfir(cfg, inbuf, outbuf, n_new, offset):
+    """kiss_fastfir (reference tools/kiss_fastfir.c:40).
+
+    ``offset`` is a one-element list (the in/out ``size_t *offset``).
+    Returns the number of output samples written."""
+    L = cfg.lib
+    _use_torch_stream(L, inbuf, outbuf)
+    off = ctypes.c_size_t(int(offset[0]))
+    n = L.kiss_fastfir_cuda(ctypes.c_void_p(cfg.ptr), _ptr(inbuf)[0], _ptr(outbuf)[0], int(n_new), ctypes.byref(off))
+    _raise_on_status(L, "kiss_fastfir")
+    offset[0] = int(off.value)
+    return int(n)
+
+
+def kiss_fastfir_filter(cfg, x, y):
+    """Whole-signal fast FIR: y[:nx-ntaps+1] = valid convolution of x with the taps."""
+    L = cfg.lib
+    _use_torch_stream(L, x, y)
+    nx = x.numel() if hasattr(x, "numel") else x.size
+    n = L.kiss_fastfir_cuda_filter(ctypes.c_void_p(cfg.ptr), _ptr(x)[0], int(nx), _ptr(y)[0])
+    _raise_on_status(L, "kiss_fastfir_filter")
+    return int(n)
+
+
+# ---------------------------------------------------------------- misc
+def last_error(dtype="float"):
+    msg = load(dtype).kiss_fft_cuda_last_error()
+    return msg.decode() if msg else ""
+
+
+def plan_info(cfg):
+    """(kind, dtype, length, hbm_passes, family, tile) of a cfg's device plan."""
+    import numpy as np
+    c = core()
+    out = (ctypes.c_int * 6)()
+    # the cfg's first field after the header is the core plan pointer
+    plan_ptr = ctypes.c_void_p.from_address(cfg.ptr + 40).value
+    c.kfg_plan_info(ctypes.c_void_p(plan_ptr), out, 6)
+    return tuple(int(v) for v in out)

@@ -1,0 +1,575 @@
+// The register-pass FFT engine (host/device code: the CUDA kernels run it,
+// and the CPU emulator used by the tests runs the very same functions).
+//
+// A sub-plan's stages are grouped into passes of one or two stages.  In a
+// pass every thread takes groups of R elements: R = p (one stage) or
+// pa*pb (two stages, run on registers without an exchange in between).
+// The first pass reads its group straight from HBM (input order is the
+// natural order of the input samples, so consecutive threads read
+// consecutive samples); the last pass writes its group straight to HBM in
+// position order (= output order).  Between passes the tile lives in shared
+// memory at index I = A*sA + job*sJ (A = input-order index), XOR-swizzled
+// so that both the input-order and the position-order sweeps are
+// bank-conflict free for power-of-two strides.
+#pragma once
+#include "kf_arith.cuh"
+#include "kf_desc.h"
+#include <string.h>
+
+namespace kf {
+
+// Read-only (non-coherent cache) load of tables: twiddles, reverse tables.
+template <typename T>
+KF_HD T ldro(const T* p) {
+#if defined(__CUDA_ARCH__)
+    T r;
+    if constexpr (sizeof(T) == 4) {
+        unsigned v = __ldg((const unsigned*)p);
+        memcpy(&r, &v, 4);
+    } else if constexpr (sizeof(T) == 8) {
+        uint2 v = __ldg((const uint2*)p);
+        memcpy(&r, &v, 8);
+    } else if constexpr (sizeof(T) == 16) {
+        uint4 v = __ldg((const uint4*)p);
+        memcpy(&r, &v, 16);
+    } else {
+        r = *p;
+    }
+    return r;
+#else
+    return *p;
+#endif
+}
+#define KF_LDG(p) ::kf::ldro(p)
+
+template <typename S>
+struct SwzBits {
+    static const int v = sizeof(cpx<S>) == 4 ? 5 : (sizeof(cpx<S>) == 8 ? 4 : 3);
+};
+
+// XOR-fold swizzle inside aligned blocks of 2^B elements (a bijection).
+template <typename S>
+KF_HD int swz(int I) {
+    const int B = SwzBits<S>::v;
+    const int f = (I >> B) ^ (I >> (2 * B)) ^ (I >> (3 * B)) ^ (I >> (4 * B));
+    return I ^ (f & ((1 << B) - 1));
+}
+
+// Per-tile view: shared tile, job table, global pointers.
+template <typename S>
+struct Tile {
+    typedef cpx<S> C;
+    C* sm;
+    int sA, sJ;  // shared index strides of the input-order index and of the job
+    int J, logJ, col;
+    int T;       // threads working on the tile
+    const long long* inb;
+    const long long* outb;
+    const int* U;
+    const long long* lim_in;   // real-input limit (fast FIR); null otherwise
+    const long long* lim_out;  // real-output limit (fast FIR)
+    const void* in;
+    void* out;
+    long long in_stride, out_stride;
+    int* err;
+
+    KF_HD int sidx(int A, int job) const { return swz<S>(A * sA + job * sJ); }
+    KF_HD C sld(int A, int job) const { return sm[sidx(A, job)]; }
+    KF_HD void sst(int A, int job, C v) const { sm[sidx(A, job)] = v; }
+    KF_HD bool valid(int job) const { return inb[job] >= 0; }
+};
+
+// ------------------------------------------------------------ global access
+// Complex load/store; MODE_FIR moves real samples with limits instead.
+template <typename S, int MODE>
+KF_HD cpx<S> gload(const Tile<S>& t, int job, int A) {
+    cpx<S> v;
+    if constexpr (MODE == MODE_FIR) {
+        const S* x = (const S*)t.in + t.inb[job];
+        long long i0 = 2LL * A;
+        long long lim = t.lim_in[job];
+        v.r = i0 < lim ? x[i0] : (S)0;
+        v.i = i0 + 1 < lim ? x[i0 + 1] : (S)0;
+    } else {
+        v = ((const cpx<S>*)t.in)[t.inb[job] + (long long)A * t.in_stride];
+    }
+    return v;
+}
+
+template <typename S, int MODE>
+KF_HD void gstore(const Tile<S>& t, int job, int pos, cpx<S> v) {
+    if constexpr (MODE == MODE_FIR) {
+        S* y = (S*)t.out + t.outb[job];
+        long long i0 = 2LL * pos;
+        long long lim = t.lim_out[job];
+        if (i0 < lim) y[i0] = v.r;
+        if (i0 + 1 < lim) y[i0 + 1] = v.i;
+    } else {
+        ((cpx<S>*)t.out)[t.outb[job] + (long long)pos * t.out_stride] = v;
+    }
+}
+
+// ------------------------------------------------------------ group decode
+struct GroupIx {
+    int job, A0, pos0, ul;
+};
+
+// gidx enumerates the groups of a pass over the whole tile: jobs fastest in
+// column mode (coalesced across jobs), digits fastest in row mode.
+// Non-last passes enumerate the lower digits in input order (conflict-free
+// shared sweeps); the last pass enumerates them in position order
+// (coalesced output) and uses the reverse table.
+KF_HD GroupIx decode(const KPass& ps, const KSub& sb, int J, int logJ, int col, bool is_last, int gidx) {
+    GroupIx g;
+    int gp = ps.H * ps.ML;
+    int r;
+    if (col) {
+        g.job = gidx & (J - 1);
+        r = gidx >> logJ;
+    } else if (J == 1) {
+        g.job = 0;
+        r = gidx;
+    } else {
+        g.job = gidx / gp;
+        r = gidx - g.job * gp;
+    }
+    int h, ulp, ul;
+    if (is_last) {
+        h = 0;
+        ul = r;
+        ulp = ps.ML > 1 ? KF_LDG(sb.rev + ps.rev_off + ul) : 0;
+    } else {
+        h = r % ps.H;
+        ulp = r / ps.H;
+        ul = ps.ML > 1 ? KF_LDG(sb.rev + ps.rev_off + ulp) : 0;
+    }
+    g.A0 = h + ulp * ps.H * ps.R;
+    g.pos0 = ul;
+    g.ul = ul;
+    return g;
+}
+
+template <typename S, int P>
+KF_HD void stage_tw(const KSub& sb, const KStage& st, int u, cpx<S>* w, cpx<S>& c0, cpx<S>& c1) {
+    const cpx<S>* tws = (const cpx<S>*)sb.tw_stage + st.tw_off;
+#pragma unroll
+    for (int q = 1; q < P; ++q) w[q - 1] = KF_LDG(tws + (q - 1) * st.m + u);
+    if constexpr (P == 3 || P == 5) c0 = KF_LDG(tws + (P - 1) * st.m);
+    if constexpr (P == 5) c1 = KF_LDG(tws + (P - 1) * st.m + 1);
+}
+
+// ------------------------------------------------------------ group kernels
+// One stage of radix P (2..5) on a group of P elements.
+template <typename S, int MODE, int P>
+KF_HD void group1(const Tile<S>& t, const KSub& sb, const KPass& ps, const GroupIx& g, int U, bool src_g,
+                  bool dst_g) {
+    typedef cpx<S> C;
+    const KStage& sa = sb.st[ps.a];
+    C x[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        int A = g.A0 + q * sa.iloc;
+        x[q] = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
+    }
+    C w[P > 1 ? P - 1 : 1], c0, c1;
+    stage_tw<S, P>(sb, sa, g.ul * sb.m_low + U, w, c0, c1);
+    bfly<S, P, 1>(x, w, c0, c1, sb.inverse != 0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        if (dst_g)
+            gstore<S, MODE>(t, g.job, g.pos0 + q * sa.mloc, x[q]);
+        else
+            t.sst(g.A0 + q * sa.iloc, g.job, x[q]);
+    }
+}
+
+// Two stages: stage a+1 (radix PB) then stage a (radix PA), element
+// (ea, eb) at register k = ea + PA*eb.
+template <typename S, int MODE, int PA, int PB>
+KF_HD void group2(const Tile<S>& t, const KSub& sb, const KPass& ps, const GroupIx& g, int U, bool src_g,
+                  bool dst_g) {
+    typedef cpx<S> C;
+    const KStage& sa = sb.st[ps.a];
+    const KStage& sbb = sb.st[ps.a + 1];
+    C x[PA * PB];
+#pragma unroll
+    for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+        for (int ea = 0; ea < PA; ++ea) {
+            int A = g.A0 + ea * sa.iloc + eb * sbb.iloc;
+            x[ea + PA * eb] = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
+        }
+    {
+        C w[PB - 1], c0, c1;
+        stage_tw<S, PB>(sb, sbb, g.ul * sb.m_low + U, w, c0, c1);
+#pragma unroll
+        for (int ea = 0; ea < PA; ++ea) bfly<S, PB, PA>(x + ea, w, c0, c1, sb.inverse != 0);
+    }
+#pragma unroll
+    for (int eb = 0; eb < PB; ++eb) {
+        C w[PA - 1], c0, c1;
+        stage_tw<S, PA>(sb, sa, (eb * sbb.mloc + g.ul) * sb.m_low + U, w, c0, c1);
+        bfly<S, PA, 1>(x + PA * eb, w, c0, c1, sb.inverse != 0);
+    }
+#pragma unroll
+    for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+        for (int ea = 0; ea < PA; ++ea) {
+            if (dst_g)
+                gstore<S, MODE>(t, g.job, g.pos0 + ea * sa.mloc + eb * sbb.mloc, x[ea + PA * eb]);
+            else
+                t.sst(g.A0 + ea * sa.iloc + eb * sbb.iloc, g.job, x[ea + PA * eb]);
+        }
+}
+
+// Generic radix P (a prime 7..31) on registers, kf_bfly_generic
+// (kiss_fft.c:192-233): output leg q1 sums legs q = 0..P-1 in order with
+// twiddle index (q*fstride*k) mod N, k = u + q1*m.
+template <typename S, int MODE, int P>
+KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KPass& ps, const GroupIx& g, int U, bool src_g,
+                  bool dst_g) {
+    typedef cpx<S> C;
+    typedef Ar<S> Arr;
+    const KStage& sa = sb.st[ps.a];
+    const C* tw = (const C*)sb.tw_full;
+    C x[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        int A = g.A0 + q * sa.iloc;
+        C v = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
+        x[q] = Arr::template fixdiv<P>(v);
+    }
+    const int u = g.ul * sb.m_low + U;
+    const int N = sb.N;
+#pragma unroll 1
+    for (int q1 = 0; q1 < P; ++q1) {
+        const int step = sa.fs * (u + q1 * sa.m);
+        int twidx = 0;
+        C acc = x[0];
+#pragma unroll
+        for (int q = 1; q < P; ++q) {
+            twidx += step;
+            if (twidx >= N) twidx -= N;
+            acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
+        }
+        if (dst_g)
+            gstore<S, MODE>(t, g.job, g.pos0 + q1 * sa.mloc, acc);
+        else
+            t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
+    }
+}
+
+// Generic radix of any size, output-parallel: every thread computes up to
+// KF_MAXO outputs into registers (reading all p legs of each), then -- after
+// a barrier the caller places -- stores them.
+template <typename S, int MODE>
+KF_HD void rtg_compute(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_last, int tid, int T,
+                       bool src_g, cpx<S>* outv) {
+    typedef cpx<S> C;
+    typedef Ar<S> Arr;
+    const KStage& sa = sb.st[ps.a];
+    const C* tw = (const C*)sb.tw_full;
+    const int p = sa.p, N = sb.N;
+    const int NG = t.J * ps.H * ps.ML;
+#pragma unroll
+    for (int i = 0; i < KF_MAXO; ++i) {
+        int o = tid + i * T;
+        if (o >= NG * p) break;
+        int q1 = o / NG, gidx = o - q1 * NG;
+        GroupIx g = decode(ps, sb, t.J, t.logJ, t.col, is_last, gidx);
+        if (!t.valid(g.job)) continue;
+        int U = t.U[g.job];
+        const int step = sa.fs * (g.ul * sb.m_low + U + q1 * sa.m);
+        int twidx = 0;
+        C v0 = src_g ? gload<S, MODE>(t, g.job, g.A0) : t.sld(g.A0, g.job);
+        C acc = Arr::fixdiv_rt(v0, p);
+        for (int q = 1; q < p; ++q) {
+            int A = g.A0 + q * sa.iloc;
+            C v = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
+            twidx += step;
+            if (twidx >= N) twidx -= N;
+            acc = c_add(acc, Arr::cmul(Arr::fixdiv_rt(v, p), KF_LDG(tw + twidx)));
+        }
+        outv[i] = acc;
+    }
+}
+
+template <typename S, int MODE>
+KF_HD void rtg_store(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_last, int tid, int T, bool dst_g,
+                     const cpx<S>* outv) {
+    const KStage& sa = sb.st[ps.a];
+    const int p = sa.p;
+    const int NG = t.J * ps.H * ps.ML;
+#pragma unroll
+    for (int i = 0; i < KF_MAXO; ++i) {
+        int o = tid + i * T;
+        if (o >= NG * p) break;
+        int q1 = o / NG, gidx = o - q1 * NG;
+        GroupIx g = decode(ps, sb, t.J, t.logJ, t.col, is_last, gidx);
+        if (!t.valid(g.job)) continue;
+        if (dst_g)
+            gstore<S, MODE>(t, g.job, g.pos0 + q1 * sa.mloc, outv[i]);
+        else
+            t.sst(g.A0 + q1 * sa.iloc, g.job, outv[i]);
+    }
+}
+
+// All groups of one (non runtime-generic) pass handled by thread tid.
+// FAM limits the pass kinds compiled in: kf_factor emits 4s, at most one 2,
+// then 3s, 5s and larger primes, so only 9 ordered radix pairs can occur.
+template <typename S, int MODE, int FAM>
+KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_last, int tid, int T, bool src_g,
+                    bool dst_g) {
+    const int NG = t.J * ps.H * ps.ML;
+    for (int gidx = tid; gidx < NG; gidx += T) {
+        GroupIx g = decode(ps, sb, t.J, t.logJ, t.col, is_last, gidx);
+        if (!t.valid(g.job)) continue;
+        const int U = t.U[g.job];
+        switch (ps.kind) {
+#define KF_G1(P) \
+    case P: group1<S, MODE, P>(t, sb, ps, g, U, src_g, dst_g); break;
+#define KF_G2(PA, PB) \
+    case 10 * PA + PB: group2<S, MODE, PA, PB>(t, sb, ps, g, U, src_g, dst_g); break;
+#define KF_GG(P) \
+    case 100 + P: groupg<S, MODE, P>(t, sb, ps, g, U, src_g, dst_g); break;
+            KF_G1(2) KF_G1(4) KF_G2(4, 2) KF_G2(4, 4)
+            case 3: case 5: case 23: case 25: case 33: case 35: case 43: case 45: case 55:
+                if constexpr (FAM >= FAM_SMOOTH) {
+                    switch (ps.kind) {
+                        KF_G1(3) KF_G1(5)
+                        KF_G2(2, 3) KF_G2(2, 5) KF_G2(3, 3) KF_G2(3, 5) KF_G2(4, 3) KF_G2(4, 5) KF_G2(5, 5)
+                    }
+                }
+                break;
+            case 107: case 111: case 113: case 117: case 119: case 123: case 129: case 131:
+                if constexpr (FAM >= FAM_GENERAL) {
+                    switch (ps.kind) {
+                        KF_GG(7) KF_GG(11) KF_GG(13) KF_GG(17) KF_GG(19) KF_GG(23) KF_GG(29) KF_GG(31)
+                    }
+                }
+                break;
+#undef KF_G1
+#undef KF_G2
+#undef KF_GG
+            default:
+                if (t.err) *t.err = 1;
+                break;
+        }
+    }
+}
+
+// ------------------------------------------------------------ real-transform phases
+// Split of kiss_fftr (kiss_fftr.c:88-116) for work item k = 0..ncfft/2 of
+// the half-size complex transform X: from Xk = X[k], Xnk = X[ncfft-k] (for
+// k == 0: X[0] twice) to the bins Fk = F[k] and Fnk = F[ncfft-k] (for
+// k == 0: F[0] and F[ncfft]).  When k == ncfft-k the reference writes the
+// bin twice and Fnk is the value that survives.
+template <typename S>
+KF_HD void split_vals(const KSub& sb, int k, cpx<S> Xk, cpx<S> Xnk, cpx<S>& Fk, cpx<S>& Fnk) {
+    typedef Ar<S> Arr;
+    typedef cpx<S> C;
+    if (k == 0) {
+        C dc = Arr::template fixdiv<2>(Xk);
+        Fk.r = Arr::st(Arr::add(dc.r, dc.i));
+        Fk.i = 0;
+        Fnk.r = Arr::st(Arr::sub(dc.r, dc.i));
+        Fnk.i = 0;
+        return;
+    }
+    C fpnk;
+    fpnk.r = Xnk.r;
+    fpnk.i = Arr::st(Arr::neg(Xnk.i));
+    C fpk = Arr::template fixdiv<2>(Xk);
+    fpnk = Arr::template fixdiv<2>(fpnk);
+    C f1k = c_add(fpk, fpnk), f2k = c_sub(fpk, fpnk);
+    C tw = Arr::cmul(f2k, KF_LDG((const C*)sb.super_tw + (k - 1)));
+    Fk.r = Arr::st(Arr::half(Arr::add(f1k.r, tw.r)));
+    Fk.i = Arr::st(Arr::half(Arr::add(f1k.i, tw.i)));
+    Fnk.r = Arr::st(Arr::half(Arr::sub(f1k.r, tw.r)));
+    Fnk.i = Arr::st(Arr::half(Arr::sub(tw.i, f1k.i)));
+}
+
+// The same split reading X from the shared tile (position n lives at
+// input-order index revfull[n]).
+template <typename S>
+KF_HD void r2c_split_pair(const Tile<S>& t, const KSub& sb, int job, int k, cpx<S>& Fk, cpx<S>& Fnk) {
+    cpx<S> Xk = t.sld(KF_LDG(sb.revfull + k), job);
+    cpx<S> Xnk = k == 0 ? Xk : t.sld(KF_LDG(sb.revfull + (sb.L - k)), job);
+    split_vals(sb, k, Xk, Xnk, Fk, Fnk);
+}
+
+// Merge of kiss_fftri (kiss_fftr.c:131-153) for work item k: from bins
+// Gk = G[k] and Gnk = G[ncfft-k] (for k == 0: G[0] and G[ncfft]) to the
+// half-size inverse input tmp[k], tmp[ncfft-k].
+template <typename S>
+KF_HD void c2r_merge_pair(const KSub& sb, int k, cpx<S> Gk, cpx<S> Gnk, cpx<S>& tk, cpx<S>& tnk) {
+    typedef Ar<S> Arr;
+    typedef cpx<S> C;
+    if (k == 0) {
+        C t0;
+        t0.r = Arr::st(Arr::add(Gk.r, Gnk.r));
+        t0.i = Arr::st(Arr::sub(Gk.r, Gnk.r));
+        tk = Arr::template fixdiv<2>(t0);
+        tnk = tk;
+        return;
+    }
+    C fk = Gk, fnkc;
+    fnkc.r = Gnk.r;
+    fnkc.i = Arr::st(Arr::neg(Gnk.i));
+    fk = Arr::template fixdiv<2>(fk);
+    fnkc = Arr::template fixdiv<2>(fnkc);
+    C fek = c_add(fk, fnkc), d = c_sub(fk, fnkc);
+    C fok = Arr::cmul(d, KF_LDG((const C*)sb.super_tw + (k - 1)));
+    tk = c_add(fek, fok);
+    tnk = c_sub(fek, fok);
+    tnk.i = Arr::st(Arr::neg(tnk.i));
+}
+
+KF_HD void item_decode(int J, int logJ, int col, int nk, int it, int& job, int& k) {
+    if (col) {
+        job = it & (J - 1);
+        k = it >> logJ;
+    } else {
+        job = it / nk;
+        k = it - job * nk;
+    }
+}
+
+// R2C: split from shared memory straight to the output bins in HBM.
+template <typename S>
+KF_HD void r2c_post(const Tile<S>& t, const KSub& sb, int tid, int T) {
+    const int ncfft = sb.L, nk = ncfft / 2 + 1;
+    for (int it = tid; it < t.J * nk; it += T) {
+        int job, k;
+        item_decode(t.J, t.logJ, t.col, nk, it, job, k);
+        if (!t.valid(job)) continue;
+        cpx<S> Fk, Fnk;
+        r2c_split_pair(t, sb, job, k, Fk, Fnk);
+        cpx<S>* o = (cpx<S>*)t.out + t.outb[job];
+        if (k != ncfft - k) o[(long long)k * t.out_stride] = Fk;
+        o[(long long)(ncfft - k) * t.out_stride] = Fnk;
+    }
+}
+
+// C2R: merge from the input bins in HBM into the shared tile (input order).
+template <typename S>
+KF_HD void c2r_pre(const Tile<S>& t, const KSub& sb, int tid, int T) {
+    const int ncfft = sb.L, nk = ncfft / 2 + 1;
+    for (int it = tid; it < t.J * nk; it += T) {
+        int job, k;
+        item_decode(t.J, t.logJ, t.col, nk, it, job, k);
+        if (!t.valid(job)) continue;
+        const cpx<S>* f = (const cpx<S>*)t.in + t.inb[job];
+        cpx<S> Gk = f[(long long)k * t.in_stride];
+        cpx<S> Gnk = f[(long long)(ncfft - k) * t.in_stride];
+        cpx<S> tk, tnk;
+        c2r_merge_pair(sb, k, Gk, Gnk, tk, tnk);
+        if (k == 0) {
+            t.sst(0, job, tk);
+        } else {
+            if (k != ncfft - k) t.sst(k, job, tk);
+            t.sst(ncfft - k, job, tnk);
+        }
+    }
+}
+
+// Fast FIR middle: split (forward plan), multiply by the filter response,
+// merge (inverse plan).  Reads every bin pair before any write: the caller
+// places a barrier between fir_mid_compute and fir_mid_store.
+template <typename S>
+KF_HD void fir_mid_compute(const Tile<S>& t, const KSub& fw, const KSub& iv, const cpx<S>* H, int tid, int T,
+                           cpx<S>* outv) {
+    typedef Ar<S> Arr;
+    const int ncfft = fw.L, nk = ncfft / 2 + 1;
+#pragma unroll
+    for (int i = 0; i < KF_MAXO / 2; ++i) {
+        int it = tid + i * T;
+        if (it >= t.J * nk) break;
+        int job, k;
+        item_decode(t.J, t.logJ, t.col, nk, it, job, k);
+        if (!t.valid(job)) continue;
+        cpx<S> Fk, Fnk;
+        r2c_split_pair(t, fw, job, k, Fk, Fnk);
+        int kk = k, knk = ncfft - k;
+        if (k == 0) kk = 0, knk = ncfft;
+        cpx<S> Gk = Arr::cmul(Fk, KF_LDG(H + kk));
+        cpx<S> Gnk = Arr::cmul(Fnk, KF_LDG(H + knk));
+        if (k != 0 && k == ncfft - k) Gk = Gnk;
+        c2r_merge_pair(iv, k, Gk, Gnk, outv[2 * i], outv[2 * i + 1]);
+    }
+}
+
+template <typename S>
+KF_HD void fir_mid_store(const Tile<S>& t, const KSub& fw, int tid, int T, const cpx<S>* outv) {
+    const int ncfft = fw.L, nk = ncfft / 2 + 1;
+#pragma unroll
+    for (int i = 0; i < KF_MAXO / 2; ++i) {
+        int it = tid + i * T;
+        if (it >= t.J * nk) break;
+        int job, k;
+        item_decode(t.J, t.logJ, t.col, nk, it, job, k);
+        if (!t.valid(job)) continue;
+        if (k == 0) {
+            t.sst(0, job, outv[2 * i]);
+        } else {
+            if (k != ncfft - k) t.sst(k, job, outv[2 * i]);
+            t.sst(ncfft - k, job, outv[2 * i + 1]);
+        }
+    }
+}
+
+// Standalone split / merge items for real plans that run as two HBM
+// passes: X (or the merged input) sits in HBM in natural order.
+template <typename S>
+KF_HD void split_item(const KArgs& a, long long it) {
+    const KSub& sb = a.sub[0];
+    const int ncfft = sb.L, nk = ncfft / 2 + 1;
+    long long b = it / nk;
+    int k = (int)(it - b * nk);
+    const cpx<S>* X = (const cpx<S>*)a.in + b * a.in_dhi;
+    cpx<S>* F = (cpx<S>*)a.out + b * a.out_dhi;
+    cpx<S> Fk, Fnk;
+    split_vals(sb, k, X[k], k == 0 ? X[0] : X[ncfft - k], Fk, Fnk);
+    if (k != ncfft - k) F[k] = Fk;
+    F[ncfft - k] = Fnk;
+}
+
+template <typename S>
+KF_HD void merge_item(const KArgs& a, long long it) {
+    const KSub& sb = a.sub[0];
+    const int ncfft = sb.L, nk = ncfft / 2 + 1;
+    long long b = it / nk;
+    int k = (int)(it - b * nk);
+    const cpx<S>* G = (const cpx<S>*)a.in + b * a.in_dhi;
+    cpx<S>* X = (cpx<S>*)a.out + b * a.out_dhi;
+    cpx<S> tk, tnk;
+    c2r_merge_pair(sb, k, G[k], G[ncfft - k], tk, tnk);
+    if (k == 0) {
+        X[0] = tk;
+    } else {
+        if (k != ncfft - k) X[k] = tk;
+        X[ncfft - k] = tnk;
+    }
+}
+
+// Job table entries for tile slot j (any thread may fill one).
+KF_HD void job_entry(const KArgs& a, long long tile, int j, long long& inb, long long& outb, int& U, long long& lin,
+                     long long& lout) {
+    long long jg = tile * a.J + j;
+    if (jg >= a.G) {
+        inb = -1;
+        outb = -1;
+        U = 0;
+        lin = lout = 0;
+        return;
+    }
+    long long ghi = jg / a.G_lo, glo = jg - ghi * a.G_lo;
+    inb = ghi * a.in_dhi + glo * a.in_dlo;
+    outb = ghi * a.out_dhi + glo * a.out_dlo;
+    U = a.use_u ? (int)glo : 0;
+    lin = a.in_limit - inb;
+    lout = a.out_limit - outb;
+    if (a.fir_ngood > 0 && lout > a.fir_ngood) lout = a.fir_ngood;
+}
+
+}  // namespace kf

@@ -1,0 +1,466 @@
+// Core library: device plans, launch-schedule execution, host staging and
+// the dtype-tagged C API of include/kissfft_gb300.h.
+//
+// Plans are immutable once built (twiddles, digit-reversal tables and the
+// launch schedule templates live in one device allocation), so one plan may
+// be used from several threads and streams at once.  Scratch for two-pass
+// plans and host staging is stream-ordered (cudaMallocAsync on the call's
+// stream), never shared between calls.
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kf_kernels.cuh"
+#include "kissfft_gb300.h"
+
+using namespace kf;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<cudaStream_t> g_stream{(cudaStream_t)0};
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define KFG_CK(call)                                                                                   \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(KFG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+enum { K_C2C = 1, K_REAL = 2, K_ND = 3, K_NDR = 4, K_FIR = 5 };
+
+struct DevPlan {
+    Plan p;
+    void* d = nullptr;
+    ~DevPlan() {
+        if (d) cudaFree(d);
+    }
+};
+
+std::unique_ptr<DevPlan> make_devplan(int dtype, int n, int inverse, int real_nfft) {
+    std::unique_ptr<DevPlan> dp(new DevPlan);
+    if (!dp->p.build(dtype, n, inverse, 0, real_nfft)) {
+        fail(KFG_EINVAL, dp->p.error);
+        return nullptr;
+    }
+    cudaError_t e = cudaMalloc(&dp->d, dp->p.blob.size());
+    if (e != cudaSuccess) {
+        fail(e == cudaErrorMemoryAllocation ? KFG_ENOMEM : KFG_ECUDA,
+             std::string("cudaMalloc(plan): ") + cudaGetErrorString(e));
+        dp->d = nullptr;
+        return nullptr;
+    }
+    e = cudaMemcpy(dp->d, dp->p.blob.data(), dp->p.blob.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        fail(KFG_ECUDA, std::string("cudaMemcpy(plan): ") + cudaGetErrorString(e));
+        return nullptr;
+    }
+    dp->p.bind(dp->d);
+    return dp;
+}
+
+bool is_device_ptr(const void* ptr) {
+    if (!ptr) return false;
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+cudaStream_t pick(void* stream) { return stream ? (cudaStream_t)stream : g_stream.load(); }
+
+// scale the fast FIR response by the reference's float(1.0/nfft)
+__global__ void kf_scale_kernel(float* H, long long n, float s) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) H[i] *= s;
+}
+
+}  // namespace
+
+struct kfg_plan {
+    int kind = 0, dtype = 0, inverse = 0;
+    long long n = 0;  // c2c: nfft; real: nfft; nd/ndr: product of dims; fir: nfft
+    std::vector<int> dims;
+    std::unique_ptr<DevPlan> main, aux;
+    std::vector<std::unique_ptr<DevPlan>> axes;  // one per axis (nd), or per leading axis (ndr)
+    long long ntaps = 0;
+    void* d_H = nullptr;
+    ~kfg_plan() {
+        if (d_H) cudaFree(d_H);
+    }
+};
+
+namespace {
+
+int run_schedule(Schedule& s, const void* in, void* out, cudaStream_t st, const void* firH = nullptr) {
+    void* scratch = nullptr;
+    const size_t off1 = (s.scratch[0] + 255) & ~(size_t)255;
+    const size_t tot = off1 + s.scratch[1];
+    if (s.scratch[0] + s.scratch[1] > 0) KFG_CK(cudaMallocAsync(&scratch, tot, st));
+    int rc = KFG_OK;
+    for (auto& step : s.steps) {
+        void* roles[4] = {(void*)in, out, scratch, (char*)scratch + off1};
+        step.args.in = roles[step.in_role];
+        step.args.out = roles[step.out_role];
+        step.args.fir_H = firH;
+        cudaError_t e = launch_step(step, st);
+        if (e != cudaSuccess) {
+            rc = fail(KFG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+            break;
+        }
+    }
+    if (scratch) cudaFreeAsync(scratch, st);
+    return rc;
+}
+
+int esz_of(int dtype) { return cpx_size(dtype); }
+
+// Build the schedule of one batched call; in/out element counts per
+// transform are returned for staging.
+int build_schedule(kfg_plan* p, long long batch, long long in_dist, long long in_stride, long long out_dist,
+                   Schedule& s, size_t& in_bytes, size_t& out_bytes) {
+    const int esz = esz_of(p->dtype), rsz = esz / 2;
+    s = Schedule();
+    switch (p->kind) {
+        case K_C2C: {
+            const long long n = p->n;
+            if (!in_dist) in_dist = n * in_stride;
+            if (!out_dist) out_dist = n;
+            if (!schedule_c2c(p->main->p, batch, in_dist, in_stride, out_dist, s)) return fail(KFG_EINVAL, s.error);
+            in_bytes = (size_t)((batch - 1) * in_dist + (n - 1) * in_stride + 1) * esz;
+            out_bytes = (size_t)((batch - 1) * out_dist + n) * esz;
+            return KFG_OK;
+        }
+        case K_REAL: {
+            const long long nfft = p->n, nb = nfft / 2 + 1;
+            if (!p->inverse) {
+                if (!in_dist) in_dist = nfft;
+                if (!out_dist) out_dist = nb;
+                if (!schedule_r2c(p->main->p, batch, in_dist, out_dist, s)) return fail(KFG_EINVAL, s.error);
+                in_bytes = (size_t)((batch - 1) * in_dist + nfft) * rsz;
+                out_bytes = (size_t)((batch - 1) * out_dist + nb) * esz;
+            } else {
+                if (!in_dist) in_dist = nb;
+                if (!out_dist) out_dist = nfft;
+                if (!schedule_c2r(p->main->p, batch, in_dist, out_dist, s)) return fail(KFG_EINVAL, s.error);
+                in_bytes = (size_t)((batch - 1) * in_dist + nb) * esz;
+                out_bytes = (size_t)((batch - 1) * out_dist + nfft) * rsz;
+            }
+            return KFG_OK;
+        }
+        case K_ND: {
+            const long long tot = p->n;
+            if ((in_dist && in_dist != tot) || (out_dist && out_dist != tot))
+                return fail(KFG_EINVAL, "N-D batches must be packed");
+            const int nd = (int)p->dims.size();
+            for (int k = 0; k < nd; ++k) {
+                Schedule a;
+                if (!schedule_axis(p->axes[k]->p, p->dims.data(), nd, k, batch, k == 0 ? 0 : 1, 1, a))
+                    return fail(KFG_EINVAL, a.error);
+                for (auto& st : a.steps) s.steps.push_back(st);
+            }
+            in_bytes = out_bytes = (size_t)(batch * tot) * esz;
+            return KFG_OK;
+        }
+        case K_NDR: {
+            const int nd = (int)p->dims.size();
+            const long long dr = p->dims[nd - 1], nb = dr / 2 + 1;
+            long long other = 1;
+            for (int i = 0; i < nd - 1; ++i) other *= p->dims[i];
+            if ((in_dist && in_dist != (p->inverse ? other * nb : other * dr)) ||
+                (out_dist && out_dist != (p->inverse ? other * dr : other * nb)))
+                return fail(KFG_EINVAL, "N-D batches must be packed");
+            std::vector<int> bd(p->dims.begin(), p->dims.end());
+            bd[nd - 1] = (int)nb;
+            if (!p->inverse) {
+                if (!schedule_r2c(p->main->p, batch * other, dr, nb, s)) return fail(KFG_EINVAL, s.error);
+                for (int k = 0; k < nd - 1; ++k) {
+                    Schedule a;
+                    if (!schedule_axis(p->axes[k]->p, bd.data(), nd, k, batch, 1, 1, a))
+                        return fail(KFG_EINVAL, a.error);
+                    for (auto& st : a.steps) s.steps.push_back(st);
+                }
+                in_bytes = (size_t)(batch * other * dr) * rsz;
+                out_bytes = (size_t)(batch * other * nb) * esz;
+            } else {
+                if (nd == 1) {
+                    if (!schedule_c2r(p->main->p, batch, nb, dr, s)) return fail(KFG_EINVAL, s.error);
+                } else {
+                    if (p->main->p.nsub != 1) return fail(KFG_EUNSUPPORTED, "N-D real inverse: last axis too long");
+                    for (int k = 0; k < nd - 1; ++k) {
+                        Schedule a;
+                        if (!schedule_axis(p->axes[k]->p, bd.data(), nd, k, batch, k == 0 ? 0 : 2, 2, a))
+                            return fail(KFG_EINVAL, a.error);
+                        for (auto& st : a.steps) s.steps.push_back(st);
+                    }
+                    Schedule c;
+                    if (!schedule_c2r(p->main->p, batch * other, nb, dr, c, 2, 1)) return fail(KFG_EINVAL, c.error);
+                    for (auto& st : c.steps) s.steps.push_back(st);
+                    s.scratch[0] = (size_t)(batch * other * nb) * esz;
+                }
+                in_bytes = (size_t)(batch * other * nb) * esz;
+                out_bytes = (size_t)(batch * other * dr) * rsz;
+            }
+            return KFG_OK;
+        }
+    }
+    return fail(KFG_EINVAL, "plan kind cannot run kfg_exec");
+}
+
+// Run a schedule with host-pointer staging where needed.
+int exec_staged(Schedule& s, const void* in, void* out, size_t in_bytes, size_t out_bytes, cudaStream_t st,
+                const void* firH = nullptr) {
+    const bool din = is_device_ptr(in), dout = is_device_ptr(out);
+    if (din && dout) return run_schedule(s, in, out, st, firH);
+    void *sin = (void*)in, *sout = out;
+    if (!din) {
+        KFG_CK(cudaMallocAsync(&sin, in_bytes, st));
+        KFG_CK(cudaMemcpyAsync(sin, in, in_bytes, cudaMemcpyHostToDevice, st));
+    }
+    if (!dout) {
+        if (!din && (const void*)out == in && out_bytes <= in_bytes)
+            sout = sin;
+        else
+            KFG_CK(cudaMallocAsync(&sout, out_bytes, st));
+    }
+    int rc = run_schedule(s, sin, sout, st, firH);
+    if (rc == KFG_OK && !dout) {
+        cudaError_t e = cudaMemcpyAsync(out, sout, out_bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) rc = fail(KFG_ECUDA, std::string("cudaMemcpyAsync(D2H): ") + cudaGetErrorString(e));
+    }
+    if (!din) cudaFreeAsync(sin, st);
+    if (!dout && sout != sin) cudaFreeAsync(sout, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == KFG_OK && e != cudaSuccess) rc = fail(KFG_ECUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+    return rc;
+}
+
+bool valid_dtype(int d) { return d >= KFG_FLOAT && d <= KFG_INT32; }
+
+}  // namespace
+
+extern "C" {
+
+kfg_plan* kfg_plan_c2c(int dtype, int nfft, int inverse) {
+    if (!valid_dtype(dtype) || nfft < 1) {
+        fail(KFG_EINVAL, "kfg_plan_c2c: bad sample type or size");
+        return nullptr;
+    }
+    std::unique_ptr<kfg_plan> p(new kfg_plan);
+    p->kind = K_C2C;
+    p->dtype = dtype;
+    p->inverse = inverse ? 1 : 0;
+    p->n = nfft;
+    p->main = make_devplan(dtype, nfft, p->inverse, 0);
+    if (!p->main) return nullptr;
+    return p.release();
+}
+
+kfg_plan* kfg_plan_real(int dtype, int nfft, int inverse) {
+    if (!valid_dtype(dtype) || nfft < 2 || (nfft & 1)) {
+        // kiss_fftr_alloc rejects odd sizes (kiss_fftr.c:29-32)
+        fail(KFG_EINVAL, "Real FFT optimization must be even.");
+        return nullptr;
+    }
+    std::unique_ptr<kfg_plan> p(new kfg_plan);
+    p->kind = K_REAL;
+    p->dtype = dtype;
+    p->inverse = inverse ? 1 : 0;
+    p->n = nfft;
+    p->main = make_devplan(dtype, nfft / 2, p->inverse, nfft);
+    if (!p->main) return nullptr;
+    return p.release();
+}
+
+kfg_plan* kfg_plan_nd(int dtype, const int* dims, int ndims, int inverse) {
+    if (!valid_dtype(dtype) || !dims || ndims < 1) {
+        fail(KFG_EINVAL, "kfg_plan_nd: bad arguments");
+        return nullptr;
+    }
+    std::unique_ptr<kfg_plan> p(new kfg_plan);
+    p->kind = K_ND;
+    p->dtype = dtype;
+    p->inverse = inverse ? 1 : 0;
+    p->n = 1;
+    for (int i = 0; i < ndims; ++i) {
+        if (dims[i] < 1) {
+            fail(KFG_EINVAL, "kfg_plan_nd: dimension < 1");
+            return nullptr;
+        }
+        p->dims.push_back(dims[i]);
+        p->n *= dims[i];
+        p->axes.push_back(make_devplan(dtype, dims[i], p->inverse, 0));
+        if (!p->axes.back()) return nullptr;
+        if (p->axes.back()->p.nsub != 1) {
+            fail(KFG_EUNSUPPORTED, "kfg_plan_nd: an axis longer than one shared-memory tile");
+            return nullptr;
+        }
+    }
+    return p.release();
+}
+
+kfg_plan* kfg_plan_ndr(int dtype, const int* dims, int ndims, int inverse) {
+    if (!valid_dtype(dtype) || !dims || ndims < 1 || dims[ndims - 1] < 2 || (dims[ndims - 1] & 1)) {
+        fail(KFG_EINVAL, "kfg_plan_ndr: bad arguments (the last dimension must be even)");
+        return nullptr;
+    }
+    std::unique_ptr<kfg_plan> p(new kfg_plan);
+    p->kind = K_NDR;
+    p->dtype = dtype;
+    p->inverse = inverse ? 1 : 0;
+    p->n = 1;
+    for (int i = 0; i < ndims; ++i) {
+        if (dims[i] < 1) {
+            fail(KFG_EINVAL, "kfg_plan_ndr: dimension < 1");
+            return nullptr;
+        }
+        p->dims.push_back(dims[i]);
+        p->n *= dims[i];
+    }
+    p->main = make_devplan(dtype, dims[ndims - 1] / 2, p->inverse, dims[ndims - 1]);
+    if (!p->main) return nullptr;
+    for (int i = 0; i < ndims - 1; ++i) {
+        p->axes.push_back(make_devplan(dtype, dims[i], p->inverse, 0));
+        if (!p->axes.back()) return nullptr;
+        if (p->axes.back()->p.nsub != 1) {
+            fail(KFG_EUNSUPPORTED, "kfg_plan_ndr: an axis longer than one shared-memory tile");
+            return nullptr;
+        }
+    }
+    return p.release();
+}
+
+kfg_plan* kfg_plan_fir(const float* taps, size_t ntaps, size_t nfft, size_t* nfft_out) {
+    if (!taps || ntaps < 1) {
+        fail(KFG_EINVAL, "kfg_plan_fir: no taps");
+        return nullptr;
+    }
+    if (nfft == 0) {
+        // block size rule of kiss_fastfir_alloc (tools/kiss_fastfir.c:75-87)
+        size_t i = ntaps - 1;
+        nfft = 2;
+        do {
+            nfft <<= 1;
+        } while (i >>= 1);
+        if (nfft < 2048) nfft = 2048;
+    }
+    if (nfft_out) *nfft_out = nfft;
+    if ((nfft & 1) || nfft < ntaps || nfft > (size_t)1 << 30) {
+        fail(KFG_EINVAL, "kfg_plan_fir: block size must be even and at least the filter length");
+        return nullptr;
+    }
+    std::unique_ptr<kfg_plan> p(new kfg_plan);
+    p->kind = K_FIR;
+    p->dtype = KFG_FLOAT;
+    p->n = (long long)nfft;
+    p->ntaps = (long long)ntaps;
+    p->main = make_devplan(KFG_FLOAT, (int)nfft / 2, 0, (int)nfft);
+    if (!p->main) return nullptr;
+    p->aux = make_devplan(KFG_FLOAT, (int)nfft / 2, 1, (int)nfft);
+    if (!p->aux) return nullptr;
+    // taps rotated left by ntaps-1 so the scrap lands at the block tail
+    // (tools/kiss_fastfir.c:142-148), transformed, scaled by float(1/nfft)
+    std::vector<float> rot(nfft, 0.0f);
+    rot[0] = taps[ntaps - 1];
+    for (size_t i = 0; i + 1 < ntaps; ++i) rot[nfft - ntaps + 1 + i] = taps[i];
+    const size_t nb = nfft / 2 + 1;
+    cudaStream_t st = g_stream.load();
+    void* d_rot = nullptr;
+    if (cudaMalloc(&p->d_H, nb * 8) != cudaSuccess || cudaMalloc(&d_rot, nfft * 4) != cudaSuccess) {
+        if (d_rot) cudaFree(d_rot);
+        fail(KFG_ENOMEM, "kfg_plan_fir: device allocation failed");
+        return nullptr;
+    }
+    int rc = KFG_OK;
+    if (cudaMemcpy(d_rot, rot.data(), nfft * 4, cudaMemcpyHostToDevice) != cudaSuccess) rc = KFG_ECUDA;
+    Schedule s;
+    if (rc == KFG_OK && !schedule_r2c(p->main->p, 1, (long long)nfft, (long long)nb, s)) rc = fail(KFG_EINVAL, s.error);
+    if (rc == KFG_OK) rc = run_schedule(s, d_rot, p->d_H, st);
+    if (rc == KFG_OK) {
+        float scale = 1.0 / (double)nfft;
+        kf_scale_kernel<<<(unsigned)((2 * nb + 255) / 256), 256, 0, st>>>((float*)p->d_H, (long long)(2 * nb), scale);
+        if (cudaStreamSynchronize(st) != cudaSuccess) rc = fail(KFG_ECUDA, "kfg_plan_fir: response kernel failed");
+    }
+    cudaFree(d_rot);
+    if (rc != KFG_OK) return nullptr;
+    return p.release();
+}
+
+void kfg_plan_free(kfg_plan* p) { delete p; }
+
+int kfg_exec_batch(kfg_plan* p, const void* in, void* out, long long batch, long long in_dist, long long out_dist,
+                   void* stream) {
+    if (!p || !in || !out || batch < 0) return fail(KFG_EINVAL, "kfg_exec_batch: bad arguments");
+    if (batch == 0) return KFG_OK;
+    if (p->kind == K_FIR) return fail(KFG_EINVAL, "use kfg_fir_filter for a fast FIR plan");
+    Schedule s;
+    size_t ib = 0, ob = 0;
+    int rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
+    if (rc) return rc;
+    return exec_staged(s, in, out, ib, ob, pick(stream));
+}
+
+int kfg_exec(kfg_plan* p, const void* in, void* out, void* stream) { return kfg_exec_batch(p, in, out, 1, 0, 0, stream); }
+
+int kfg_exec_stride(kfg_plan* p, const void* in, void* out, int in_stride, void* stream) {
+    if (!p || !in || !out || in_stride < 1) return fail(KFG_EINVAL, "kfg_exec_stride: bad arguments");
+    if (p->kind != K_C2C) return fail(KFG_EINVAL, "kfg_exec_stride needs a complex 1-D plan");
+    Schedule s;
+    size_t ib = 0, ob = 0;
+    int rc = build_schedule(p, 1, 0, in_stride, 0, s, ib, ob);
+    if (rc) return rc;
+    return exec_staged(s, in, out, ib, ob, pick(stream));
+}
+
+int kfg_fir_filter(kfg_plan* p, const float* x, size_t nx, float* y, size_t* ny_out, void* stream) {
+    if (!p || p->kind != K_FIR || !x || !y) return fail(KFG_EINVAL, "kfg_fir_filter: bad arguments");
+    if ((long long)nx < p->ntaps - 1) return fail(KFG_EINVAL, "kfg_fir_filter: signal shorter than the filter transient");
+    const long long nout = (long long)nx - p->ntaps + 1;
+    if (ny_out) *ny_out = (size_t)nout;
+    if (nout == 0) return KFG_OK;
+    Schedule s;
+    if (!schedule_fastfir(p->main->p, p->aux->p, p->ntaps, (long long)nx, 0, s)) return fail(KFG_EINVAL, s.error);
+    return exec_staged(s, x, y, nx * sizeof(float), (size_t)nout * sizeof(float), pick(stream), p->d_H);
+}
+
+int kfg_set_stream(void* stream) {
+    g_stream.store((cudaStream_t)stream);
+    return KFG_OK;
+}
+
+void* kfg_get_stream(void) { return (void*)g_stream.load(); }
+
+int kfg_synchronize(void) {
+    KFG_CK(cudaStreamSynchronize(g_stream.load()));
+    return KFG_OK;
+}
+
+const char* kfg_last_error(void) { return g_err.c_str(); }
+
+int kfg_next_fast_size(int n) { return next_fast_size(n); }
+
+int kfg_plan_info(const kfg_plan* p, int* out, int nout) {
+    if (!p || !out) return KFG_EINVAL;
+    int v[6] = {p->kind, p->dtype, (int)p->n, 0, 0, 0};
+    const DevPlan* d = p->main ? p->main.get() : (p->axes.empty() ? nullptr : p->axes[0].get());
+    if (d) {
+        v[3] = d->p.nsub;
+        v[4] = sub_family(d->p.sub[0]);
+        v[5] = d->p.sub[0].L;
+    }
+    for (int i = 0; i < nout && i < 6; ++i) out[i] = v[i];
+    return KFG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,638 @@
+// Host-side plans and launch schedules.  Compiled with -ffp-contract=off:
+// the twiddle expressions must round exactly like the reference's.
+#include "kf_plan.h"
+
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+
+namespace kf {
+
+int dtype_size(int dtype) {
+    switch (dtype) {
+        case KF_F32: return 4;
+        case KF_F64: return 8;
+        case KF_Q15: return 2;
+        case KF_Q31: return 4;
+    }
+    return 0;
+}
+
+std::vector<int> factor(int n) {
+    std::vector<int> f;
+    if (n <= 1) {
+        f.push_back(1);
+        return f;
+    }
+    int p = 4;
+    const double lim = floor(sqrt((double)n));
+    while (n > 1) {
+        while (n % p) {
+            p = (p == 4) ? 2 : (p == 2 ? 3 : p + 2);
+            if (p > lim) p = n;
+        }
+        n /= p;
+        f.push_back(p);
+    }
+    return f;
+}
+
+int next_fast_size(int n) {
+    for (;; ++n) {
+        int m = n;
+        while (m % 2 == 0) m /= 2;
+        while (m % 3 == 0) m /= 3;
+        while (m % 5 == 0) m /= 5;
+        if (m <= 1) return n;
+    }
+}
+
+// kf_cexp with KISS_FFT_COS/SIN (_kiss_fft_guts.h:127-145) at the plan dtype
+static void cexp_at(int dtype, double phase, void* out, size_t i) {
+    switch (dtype) {
+        case KF_F32: {
+            float* o = (float*)out + 2 * i;
+            o[0] = (float)cos(phase);
+            o[1] = (float)sin(phase);
+            break;
+        }
+        case KF_F64: {
+            double* o = (double*)out + 2 * i;
+            o[0] = cos(phase);
+            o[1] = sin(phase);
+            break;
+        }
+        case KF_Q15: {
+            int16_t* o = (int16_t*)out + 2 * i;
+            o[0] = (int16_t)floor(.5 + 32767 * cos(phase));
+            o[1] = (int16_t)floor(.5 + 32767 * sin(phase));
+            break;
+        }
+        case KF_Q31: {
+            int32_t* o = (int32_t*)out + 2 * i;
+            o[0] = (int32_t)floor(.5 + 2147483647 * cos(phase));
+            o[1] = (int32_t)floor(.5 + 2147483647 * sin(phase));
+            break;
+        }
+    }
+}
+
+// The phase expressions of kiss_fft.c:361-367 and kiss_fftr.c:53-59, kept
+// verbatim in form so that they round identically.
+void make_twiddles(int dtype, int n, int inverse, void* out) {
+    for (int i = 0; i < n; ++i) {
+        const double pi = 3.141592653589793238462643383279502884197169399375105820974944;
+        double phase = -2 * pi * i / n;
+        if (inverse) phase *= -1;
+        cexp_at(dtype, phase, out, (size_t)i);
+    }
+}
+
+void make_super_twiddles(int dtype, int ncfft, int inverse, void* out) {
+    for (int i = 0; i < ncfft / 2; ++i) {
+        double phase = -3.14159265358979323846264338327 * ((double)(i + 1) / ncfft + .5);
+        if (inverse) phase *= -1;
+        cexp_at(dtype, phase, out, (size_t)i);
+    }
+}
+
+int max_tile_len(int dtype) {
+    // one tile of at most 128 KiB of shared memory
+    return (128 * 1024) / cpx_size(dtype);
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static bool is_small_prime(int p) {
+    return p == 7 || p == 11 || p == 13 || p == 17 || p == 19 || p == 23 || p == 29 || p == 31;
+}
+
+// Build sub-plan over global stages [g0, g1).
+static void build_sub(KSub& sb, int n, int inverse, const std::vector<int>& rad, const std::vector<int>& m,
+                      const std::vector<int>& fs, const std::vector<int>& twoff, int g0, int g1,
+                      std::vector<int>& rev, int pair_rmax) {
+    memset(&sb, 0, sizeof(sb));
+    const int nst = g1 - g0;
+    sb.N = n;
+    sb.nst = nst;
+    sb.inverse = inverse;
+    sb.m_low = m[g1 - 1];
+    long long L = 1;
+    for (int j = g0; j < g1; ++j) L *= rad[j];
+    sb.L = (int)L;
+    for (int i = 0; i < nst; ++i) {
+        int j = g0 + i;
+        KStage& s = sb.st[i];
+        s.p = rad[j];
+        s.m = m[j];
+        s.fs = fs[j];
+        s.tw_off = twoff[j];
+        s.mloc = m[j] / sb.m_low;
+        s.iloc = fs[j] / fs[g0];
+    }
+    // passes, execution order: from the leaf stage down to stage 0
+    std::vector<KPass> ps;
+    int i = nst - 1;
+    while (i >= 0) {
+        KPass p;
+        memset(&p, 0, sizeof(p));
+        int pa = sb.st[i].p;
+        if (i >= 1 && pa >= 2 && pa <= 5 && sb.st[i - 1].p >= 2 && sb.st[i - 1].p <= 5 &&
+            pa * sb.st[i - 1].p <= pair_rmax) {
+            p.a = i - 1;
+            p.ns = 2;
+            p.kind = 10 * sb.st[i - 1].p + pa;
+            p.R = sb.st[i - 1].p * pa;
+            i -= 2;
+        } else {
+            p.a = i;
+            p.ns = 1;
+            // p == 1 only for nfft == 1: the reference's p = 1 generic butterfly
+            p.kind = (pa >= 2 && pa <= 5) ? pa : (is_small_prime(pa) ? 100 + pa : KIND_RT_GENERIC);
+            p.R = pa;
+            i -= 1;
+        }
+        ps.push_back(p);
+    }
+    sb.npass = (int)ps.size();
+    for (int k = 0; k < sb.npass; ++k) {
+        KPass& p = ps[k];
+        const int b = p.a + p.ns - 1;
+        p.H = sb.st[p.a].iloc;
+        p.ML = sb.st[b].mloc;
+        p.rev_off = -1;
+        const bool last = (k == sb.npass - 1);
+        if (p.ML > 1) {
+            p.rev_off = (int)rev.size();
+            rev.resize(rev.size() + p.ML);
+            for (int idx = 0; idx < p.ML; ++idx) {
+                int rem = idx, ul = 0;
+                for (int j = b + 1; j < nst; ++j) {
+                    int d = rem % sb.st[j].p;
+                    rem /= sb.st[j].p;
+                    ul += d * sb.st[j].mloc;
+                }
+                // idx is the input-order index ulp; ul its position
+                if (last)
+                    rev[p.rev_off + ul] = idx;
+                else
+                    rev[p.rev_off + idx] = ul;
+            }
+        }
+        sb.ps[k] = p;
+    }
+}
+
+static int build_revfull(KSub& sb, std::vector<int>& rev) {
+    int off = (int)rev.size();
+    rev.resize(rev.size() + sb.L);
+    for (int A = 0; A < sb.L; ++A) {
+        int rem = A, pos = 0;
+        for (int j = 0; j < sb.nst; ++j) {
+            int d = rem % sb.st[j].p;
+            rem /= sb.st[j].p;
+            pos += d * sb.st[j].mloc;
+        }
+        rev[off + pos] = A;
+    }
+    return off;
+}
+
+bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
+    dtype = dtype_;
+    n = n_;
+    inverse = inverse_ ? 1 : 0;
+    real_nfft = real_nfft_;
+    error.clear();
+    if (n < 1) {
+        error = "transform length must be positive";
+        return false;
+    }
+    if (dtype_size(dtype) == 0) {
+        error = "unknown sample type";
+        return false;
+    }
+    if (lmax <= 0) lmax = max_tile_len(dtype);
+    radix = factor(n);
+    const int K = (int)radix.size();
+    if (K > KF_MAXST) {
+        error = "too many factors";
+        return false;
+    }
+    std::vector<int> m(K), fs(K), twoff(K, -1);
+    {
+        long long f = 1;
+        for (int j = 0; j < K; ++j) {
+            fs[j] = (int)f;
+            f *= radix[j];
+            m[j] = (int)(n / f);
+        }
+    }
+    const int esz = cpx_size(dtype);
+    std::vector<uint8_t> twf((size_t)n * esz);
+    make_twiddles(dtype, n, inverse, twf.data());
+    // compact per-stage tables: (q, u) -> tw[q*u*fs], plus the radix-3/5 constants
+    std::vector<uint8_t> tws;
+    size_t cnt = 0;
+    for (int j = 0; j < K; ++j) {
+        int p = radix[j];
+        if (p > 5) continue;
+        twoff[j] = (int)cnt;
+        cnt += (size_t)(p - 1) * m[j] + 2;
+    }
+    tws.resize(std::max<size_t>(cnt, 1) * esz);
+    for (int j = 0; j < K; ++j) {
+        int p = radix[j];
+        if (p > 5) continue;
+        uint8_t* base = tws.data() + (size_t)twoff[j] * esz;
+        for (int q = 1; q < p; ++q)
+            for (int u = 0; u < m[j]; ++u)
+                memcpy(base + ((size_t)(q - 1) * m[j] + u) * esz, twf.data() + (size_t)q * u * fs[j] * esz, esz);
+        uint8_t* cst = base + (size_t)(p - 1) * m[j] * esz;
+        memcpy(cst, twf.data() + ((size_t)fs[j] * m[j] % n) * esz, esz);
+        memcpy(cst + esz, twf.data() + ((size_t)2 * fs[j] * m[j] % n) * esz, esz);
+    }
+    // split into one or two sub-plans; two-stage register groups hold up
+    // to 25 elements (16 for double, whose elements take 4 registers)
+    const int prm = dtype == KF_F64 ? 16 : 25;
+    std::vector<int> rev;
+    if (n <= lmax) {
+        nsub = 1;
+        split = 0;
+        build_sub(sub[0], n, inverse, radix, m, fs, twoff, 0, K, rev, prm);
+    } else {
+        int best = -1;
+        long long bestv = 0;
+        long long P = 1;
+        for (int s = 1; s < K; ++s) {
+            P *= radix[s - 1];
+            long long LA = n / P;
+            if (P <= lmax && LA <= lmax) {
+                long long v = std::max(P, LA);
+                if (best < 0 || v < bestv) best = s, bestv = v;
+            }
+        }
+        if (best < 0) {
+            error = "transform length has no split into two tiles of at most " + std::to_string(lmax);
+            return false;
+        }
+        nsub = 2;
+        split = best;
+        build_sub(sub[0], n, inverse, radix, m, fs, twoff, best, K, rev, prm);
+        build_sub(sub[1], n, inverse, radix, m, fs, twoff, 0, best, rev, prm);
+    }
+    for (int s = 0; s < nsub; ++s) {
+        for (int k = 0; k < sub[s].npass; ++k)
+            if (sub[s].ps[k].kind == KIND_RT_GENERIC && sub[s].L > KF_MAXO * KF_MAXT) {
+                error = "generic radix tile too long";
+                return false;
+            }
+        revfull_off[s] = nsub == 1 ? build_revfull(sub[s], rev) : -1;
+    }
+    std::vector<uint8_t> sup;
+    if (real_nfft > 0) {
+        sup.resize((size_t)std::max(1, n / 2) * esz);
+        make_super_twiddles(dtype, n, inverse, sup.data());
+    }
+    // blob
+    off_tw_full = 0;
+    off_tw_stage = align256(twf.size());
+    off_super = off_tw_stage + align256(tws.size());
+    off_rev = off_super + align256(sup.size());
+    blob.assign(off_rev + align256(std::max<size_t>(rev.size(), 1) * sizeof(int)), 0);
+    memcpy(blob.data() + off_tw_full, twf.data(), twf.size());
+    memcpy(blob.data() + off_tw_stage, tws.data(), tws.size());
+    if (!sup.empty()) memcpy(blob.data() + off_super, sup.data(), sup.size());
+    if (!rev.empty()) memcpy(blob.data() + off_rev, rev.data(), rev.size() * sizeof(int));
+    for (int s = 0; s < nsub; ++s) {
+        sub[s].tw_full = (const void*)(uintptr_t)off_tw_full;
+        sub[s].tw_stage = (const void*)(uintptr_t)off_tw_stage;
+        sub[s].super_tw = real_nfft > 0 ? (const void*)(uintptr_t)off_super : nullptr;
+        sub[s].rev = (const int*)(uintptr_t)off_rev;
+    }
+    return true;
+}
+
+void Plan::bind(const void* base) {
+    const uint8_t* b = (const uint8_t*)base;
+    for (int s = 0; s < nsub; ++s) {
+        sub[s].tw_full = b + off_tw_full;
+        sub[s].tw_stage = b + off_tw_stage;
+        sub[s].super_tw = real_nfft > 0 ? (const void*)(b + off_super) : nullptr;
+        sub[s].rev = (const int*)(b + off_rev);
+        sub[s].revfull = revfull_off[s] >= 0 ? (const int*)(b + off_rev) + revfull_off[s] : nullptr;
+    }
+}
+
+// ------------------------------------------------------------- launch shapes
+int cfg_smem_bytes(const KSub& sb, int dtype, int J) {
+    const int esz = cpx_size(dtype);
+    const int B = esz == 4 ? 5 : (esz == 8 ? 4 : 3);
+    long long e = (long long)J * sb.L;
+    e = (e + (1 << B) - 1) >> B << B;
+    return (int)(e * esz);
+}
+
+static int max_R(const KSub& sb) {
+    int r = 1;
+    for (int k = 0; k < sb.npass; ++k) r = std::max(r, sb.ps[k].R);
+    return r;
+}
+
+int cfg_min_threads(const KSub& sb, int mode, int J) {
+    long long t = 32;
+    for (int k = 0; k < sb.npass; ++k)
+        if (sb.ps[k].kind == KIND_RT_GENERIC) t = std::max<long long>(t, ((long long)J * sb.L + KF_MAXO - 1) / KF_MAXO);
+    if (mode == MODE_FIR) t = std::max<long long>(t, ((long long)J * (sb.L / 2 + 1) + KF_MAXO / 2 - 1) / (KF_MAXO / 2));
+    return (int)((t + 31) / 32 * 32);
+}
+
+LaunchCfg default_cfg(const KSub& sb, int dtype, int mode, long long G, int col_in, int col_out, int want_threads) {
+    LaunchCfg c;
+    c.col_in = col_in;
+    c.col_out = col_out;
+    const int R = max_R(sb);
+    const long long tpj = std::max(1, sb.L / R);
+    const int budget = 96 * 1024;
+    int J = 1;
+    const bool col = col_in || col_out;
+    while (J * 2 <= KF_MAXJ && J * 2 <= std::max<long long>(1, G) && cfg_smem_bytes(sb, dtype, J * 2) <= budget &&
+           (tpj * J * 2 <= want_threads || (col && J < 16)))
+        J *= 2;
+    while (J > 1 && cfg_min_threads(sb, mode, J) > KF_MAXT) J /= 2;
+    c.J = J;
+    long long T = (tpj * J + 31) / 32 * 32;
+    T = std::max<long long>(T, cfg_min_threads(sb, mode, J));
+    T = std::min<long long>(std::max<long long>(T, 32), KF_MAXT);
+    c.T = (int)T;
+    c.smem = cfg_smem_bytes(sb, dtype, J);
+    c.grid = (G + J - 1) / J;
+    return c;
+}
+
+// ------------------------------------------------------------- schedules
+static KArgs base_args(const KSub& sb) {
+    KArgs a;
+    memset(&a, 0, sizeof(a));
+    a.sub[0] = sb;
+    a.nsub = 1;
+    return a;
+}
+
+int sub_family(const KSub& sb) {
+    int f = FAM_POW2;
+    for (int k = 0; k < sb.npass; ++k) {
+        int kd = sb.ps[k].kind;
+        if (kd == 2 || kd == 4 || kd == 42 || kd == 44) continue;
+        if (kd < 99) f = std::max(f, (int)FAM_SMOOTH);
+        else f = FAM_GENERAL;
+    }
+    return f;
+}
+
+static void finish(Step& st, const LaunchCfg& c) {
+    st.fam = sub_family(st.args.sub[0]);
+    if (st.args.nsub > 1) st.fam = std::max(st.fam, sub_family(st.args.sub[1]));
+    st.cfg = c;
+    st.args.J = c.J;
+    st.args.col_in = c.col_in;
+    st.args.col_out = c.col_out;
+    int lj = 0;
+    while ((1 << lj) < c.J) ++lj;
+    st.args.logJ = lj;
+    st.args.ntiles = c.grid;
+}
+
+bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long in_stride, long long out_dist,
+                  Schedule& s) {
+    s.steps.clear();
+    s.scratch[0] = s.scratch[1] = 0;
+    const int esz = cpx_size(p.dtype);
+    if (p.nsub == 1) {
+        Step st;
+        st.mode = MODE_C2C;
+        st.dtype = p.dtype;
+        st.args = base_args(p.sub[0]);
+        st.args.G = batch;
+        st.args.G_lo = 1;
+        st.args.in_dhi = in_dist;
+        st.args.in_stride = in_stride;
+        st.args.out_dhi = out_dist;
+        st.args.out_stride = 1;
+        finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2C, batch, 0, 0));
+        s.steps.push_back(st);
+        return true;
+    }
+    const long long Ps = p.sub[1].L, LA = p.sub[0].L, n = p.n;
+    Step a;
+    a.mode = MODE_C2C;
+    a.dtype = p.dtype;
+    a.args = base_args(p.sub[0]);
+    a.args.G = batch * Ps;
+    a.args.G_lo = Ps;
+    a.args.in_dhi = in_dist;
+    a.args.in_dlo = in_stride;
+    a.args.in_stride = Ps * in_stride;
+    a.args.out_dhi = n;
+    a.args.out_dlo = 1;
+    a.args.out_stride = Ps;
+    a.in_role = 0;
+    a.out_role = 2;
+    finish(a, default_cfg(p.sub[0], p.dtype, MODE_C2C, a.args.G, 1, 1));
+    Step b;
+    b.mode = MODE_C2C;
+    b.dtype = p.dtype;
+    b.args = base_args(p.sub[1]);
+    b.args.G = batch * LA;
+    b.args.G_lo = LA;
+    b.args.in_dhi = n;
+    b.args.in_dlo = Ps;
+    b.args.in_stride = 1;
+    b.args.out_dhi = out_dist;
+    b.args.out_dlo = 1;
+    b.args.out_stride = LA;
+    b.args.use_u = 1;
+    b.in_role = 2;
+    b.out_role = 1;
+    finish(b, default_cfg(p.sub[1], p.dtype, MODE_C2C, b.args.G, 0, 1));
+    s.steps.push_back(a);
+    s.steps.push_back(b);
+    s.scratch[0] = (size_t)batch * n * esz;
+    return true;
+}
+
+// Real split / merge as separate elementwise launches (two-pass real plans).
+static Step elementwise(int kind, const Plan& p, long long batch, long long in_dist, long long out_dist, int in_role,
+                        int out_role) {
+    Step st;
+    st.kind = kind;
+    st.dtype = p.dtype;
+    st.args = base_args(p.sub[0]);
+    st.args.sub[0].L = p.n;  // ncfft for the element kernels
+    st.args.G = batch;
+    st.args.in_dhi = in_dist;
+    st.args.out_dhi = out_dist;
+    st.in_role = in_role;
+    st.out_role = out_role;
+    long long items = batch * (p.n / 2 + 1);
+    st.cfg.T = 256;
+    st.cfg.grid = (items + 255) / 256;
+    st.cfg.J = 1;
+    st.args.ntiles = st.cfg.grid;
+    return st;
+}
+
+bool schedule_r2c(const Plan& p, long long batch, long long in_dist, long long out_dist, Schedule& s, int in_role,
+                  int out_role) {
+    s.steps.clear();
+    s.scratch[0] = s.scratch[1] = 0;
+    if (p.real_nfft <= 0 || (in_dist & 1)) {
+        s.error = "real transform needs a real plan and an even row distance";
+        return false;
+    }
+    const int esz = cpx_size(p.dtype);
+    if (p.nsub == 1) {
+        Step st;
+        st.mode = MODE_R2C;
+        st.dtype = p.dtype;
+        st.args = base_args(p.sub[0]);
+        st.args.G = batch;
+        st.args.G_lo = 1;
+        st.args.in_dhi = in_dist / 2;
+        st.args.in_stride = 1;
+        st.args.out_dhi = out_dist;
+        st.args.out_stride = 1;
+        st.in_role = in_role;
+        st.out_role = out_role;
+        finish(st, default_cfg(p.sub[0], p.dtype, MODE_R2C, batch, 0, 0));
+        s.steps.push_back(st);
+        return true;
+    }
+    Schedule c;
+    schedule_c2c(p, batch, in_dist / 2, 1, p.n, c);
+    c.steps.front().in_role = in_role;
+    c.steps.back().out_role = 3;
+    for (auto& st : c.steps) s.steps.push_back(st);
+    s.steps.push_back(elementwise(1, p, batch, p.n, out_dist, 3, out_role));
+    s.scratch[0] = c.scratch[0];
+    s.scratch[1] = (size_t)batch * p.n * esz;
+    return true;
+}
+
+bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long out_dist, Schedule& s, int in_role,
+                  int out_role) {
+    s.steps.clear();
+    s.scratch[0] = s.scratch[1] = 0;
+    if (p.real_nfft <= 0 || (out_dist & 1)) {
+        s.error = "real transform needs a real plan and an even row distance";
+        return false;
+    }
+    const int esz = cpx_size(p.dtype);
+    if (p.nsub == 1) {
+        Step st;
+        st.mode = MODE_C2R;
+        st.dtype = p.dtype;
+        st.args = base_args(p.sub[0]);
+        st.args.G = batch;
+        st.args.G_lo = 1;
+        st.args.in_dhi = in_dist;
+        st.args.in_stride = 1;
+        st.args.out_dhi = out_dist / 2;
+        st.args.out_stride = 1;
+        st.in_role = in_role;
+        st.out_role = out_role;
+        finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2R, batch, 0, 0));
+        s.steps.push_back(st);
+        return true;
+    }
+    s.steps.push_back(elementwise(2, p, batch, in_dist, p.n, in_role, 3));
+    Schedule c;
+    schedule_c2c(p, batch, p.n, 1, out_dist / 2, c);
+    c.steps.front().in_role = 3;
+    c.steps.back().out_role = out_role;
+    for (auto& st : c.steps) s.steps.push_back(st);
+    s.scratch[0] = c.scratch[0];
+    s.scratch[1] = (size_t)batch * p.n * esz;
+    return true;
+}
+
+bool schedule_axis(const Plan& p, const int* dims, int ndims, int axis, long long batch, int in_role, int out_role,
+                   Schedule& s) {
+    s.steps.clear();
+    s.scratch[0] = s.scratch[1] = 0;
+    if (p.nsub != 1) {
+        s.error = "N-D axis longer than one tile is not supported";
+        return false;
+    }
+    long long S = 1, outer = batch;
+    for (int i = axis + 1; i < ndims; ++i) S *= dims[i];
+    for (int i = 0; i < axis; ++i) outer *= dims[i];
+    const long long n = dims[axis];
+    Step st;
+    st.mode = MODE_C2C;
+    st.dtype = p.dtype;
+    st.args = base_args(p.sub[0]);
+    st.in_role = in_role;
+    st.out_role = out_role;
+    if (S == 1) {
+        st.args.G = outer;
+        st.args.G_lo = 1;
+        st.args.in_dhi = n;
+        st.args.in_stride = 1;
+        st.args.out_dhi = n;
+        st.args.out_stride = 1;
+        finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2C, st.args.G, 0, 0));
+    } else {
+        st.args.G = outer * S;
+        st.args.G_lo = S;
+        st.args.in_dhi = n * S;
+        st.args.in_dlo = 1;
+        st.args.in_stride = S;
+        st.args.out_dhi = n * S;
+        st.args.out_dlo = 1;
+        st.args.out_stride = S;
+        finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2C, st.args.G, 1, 1));
+    }
+    s.steps.push_back(st);
+    return true;
+}
+
+bool schedule_fastfir(const Plan& fw, const Plan& iv, long long L, long long Ns, long long, Schedule& s) {
+    s.steps.clear();
+    s.scratch[0] = s.scratch[1] = 0;
+    const long long nfft = fw.real_nfft;
+    if (fw.nsub != 1 || iv.nsub != 1 || nfft <= 0) {
+        s.error = "fast FIR block does not fit one tile";
+        return false;
+    }
+    if (sub_family(fw.sub[0]) > FAM_SMOOTH) {
+        s.error = "fast FIR block size must have only the factors 2, 3 and 5";
+        return false;
+    }
+    const long long ngood = nfft - L + 1, nout = Ns - L + 1;
+    if (ngood < 1 || nout < 0) {
+        s.error = "bad fast FIR sizes";
+        return false;
+    }
+    Step st;
+    st.mode = MODE_FIR;
+    st.dtype = fw.dtype;
+    st.args = base_args(fw.sub[0]);
+    st.args.sub[1] = iv.sub[0];
+    st.args.nsub = 2;
+    st.args.G = (nout + ngood - 1) / ngood;
+    st.args.G_lo = 1;
+    st.args.in_dhi = ngood;
+    st.args.in_stride = 1;
+    st.args.out_dhi = ngood;
+    st.args.out_stride = 1;
+    st.args.in_limit = Ns;
+    st.args.out_limit = nout;
+    st.args.fir_ngood = (int)ngood;
+    finish(st, default_cfg(fw.sub[0], fw.dtype, MODE_FIR, st.args.G, 0, 0));
+    if (st.args.G > 0) s.steps.push_back(st);
+    return true;
+}
+
+}  // namespace kf

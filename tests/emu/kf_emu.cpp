@@ -1,0 +1,201 @@
+// CPU emulator of the GPU engine -- test infrastructure.
+//
+// Runs the library's launch schedules with the very same engine functions
+// the CUDA kernels run (kissfft_gb300/csrc/kf_engine.cuh), looping over the
+// thread indices of each CTA in order.  The tests compare its output with
+// the oracle, bit for bit in fixed point, to validate the plan tables, the
+// pass grouping, the digit-reversal addressing and the two-pass splits
+// without a GPU.  It is never part of the shipped library.
+#include <string.h>
+
+#include <vector>
+
+#include "kf_plan.h"
+#include "kf_runner.cuh"
+
+using namespace kf;
+
+static int g_force_J = 0, g_force_T = 0;
+
+template <typename S, int MODE, int FAM>
+struct CpuExec {
+    int T;
+    void sync() {}
+    void pass(Tile<S>& t, const KSub& sb, const KPass& ps, bool last, bool sg, bool dg) {
+        for (int tid = 0; tid < T; ++tid) run_pass<S, MODE, FAM>(t, sb, ps, last, tid, T, sg, dg);
+    }
+    void rtg(Tile<S>& t, const KSub& sb, const KPass& ps, bool last, bool sg, bool dg) {
+        std::vector<cpx<S>> buf((size_t)T * KF_MAXO);
+        for (int tid = 0; tid < T; ++tid) rtg_compute<S, MODE>(t, sb, ps, last, tid, T, sg, &buf[(size_t)tid * KF_MAXO]);
+        for (int tid = 0; tid < T; ++tid) rtg_store<S, MODE>(t, sb, ps, last, tid, T, dg, &buf[(size_t)tid * KF_MAXO]);
+    }
+    void c2r_pre(Tile<S>& t, const KSub& sb) {
+        for (int tid = 0; tid < T; ++tid) kf::c2r_pre<S>(t, sb, tid, T);
+    }
+    void r2c_post(Tile<S>& t, const KSub& sb) {
+        for (int tid = 0; tid < T; ++tid) kf::r2c_post<S>(t, sb, tid, T);
+    }
+    void fir_mid(Tile<S>& t, const KSub& fw, const KSub& iv, const cpx<S>* H) {
+        std::vector<cpx<S>> buf((size_t)T * KF_MAXO);
+        for (int tid = 0; tid < T; ++tid) fir_mid_compute<S>(t, fw, iv, H, tid, T, &buf[(size_t)tid * KF_MAXO]);
+        for (int tid = 0; tid < T; ++tid) fir_mid_store<S>(t, fw, tid, T, &buf[(size_t)tid * KF_MAXO]);
+    }
+};
+
+template <typename S, int MODE, int FAM>
+static int run_engine_step_f(const Step& st) {
+    const KArgs& a = st.args;
+    const LaunchCfg& c = st.cfg;
+    std::vector<cpx<S>> sm(c.smem / sizeof(cpx<S>) + 1);
+    long long inb[KF_MAXJ], outb[KF_MAXJ], lin[KF_MAXJ], lout[KF_MAXJ];
+    int U[KF_MAXJ];
+    int err = 0;
+    Tile<S> t;
+    memset(&t, 0, sizeof(t));
+    tile_layout(a, t);
+    t.sm = sm.data();
+    t.T = c.T;
+    t.inb = inb;
+    t.outb = outb;
+    t.U = U;
+    t.lim_in = lin;
+    t.lim_out = lout;
+    t.err = &err;
+    CpuExec<S, MODE, FAM> x;
+    x.T = c.T;
+    for (long long tile = 0; tile < a.ntiles; ++tile) {
+        for (int j = 0; j < a.J; ++j) job_entry(a, tile, j, inb[j], outb[j], U[j], lin[j], lout[j]);
+        run_tile<S, MODE, FAM>(x, a, t);
+    }
+    return err;
+}
+
+template <typename S, int MODE>
+static int run_engine_step(const Step& st) {
+    switch (st.fam) {
+        case FAM_POW2: return run_engine_step_f<S, MODE, FAM_POW2>(st);
+        case FAM_SMOOTH: return run_engine_step_f<S, MODE, FAM_SMOOTH>(st);
+        default: return run_engine_step_f<S, MODE, FAM_GENERAL>(st);
+    }
+}
+
+template <typename S>
+static int run_step_t(const Step& st) {
+    if (st.kind == 1) {
+        long long items = st.args.G * (st.args.sub[0].L / 2 + 1);
+        for (long long it = 0; it < items; ++it) split_item<S>(st.args, it);
+        return 0;
+    }
+    if (st.kind == 2) {
+        long long items = st.args.G * (st.args.sub[0].L / 2 + 1);
+        for (long long it = 0; it < items; ++it) merge_item<S>(st.args, it);
+        return 0;
+    }
+    switch (st.mode) {
+        case MODE_C2C: return run_engine_step<S, MODE_C2C>(st);
+        case MODE_R2C: return run_engine_step<S, MODE_R2C>(st);
+        case MODE_C2R: return run_engine_step<S, MODE_C2R>(st);
+        case MODE_FIR: return run_engine_step<S, MODE_FIR>(st);
+    }
+    return -1;
+}
+
+static int run_schedule(Schedule& s, const void* in, void* out, const void* firH = nullptr) {
+    std::vector<uint8_t> tmp(s.scratch[0] + s.scratch[1] + 16);
+    for (auto& st : s.steps) {
+        void* roles[4] = {(void*)in, out, tmp.data(), tmp.data() + s.scratch[0]};
+        st.args.in = roles[st.in_role];
+        st.args.out = roles[st.out_role];
+        st.args.fir_H = firH;
+        if (g_force_J && st.kind == 0) {
+            st.cfg.J = g_force_J;
+            st.args.J = g_force_J;
+            int lj = 0;
+            while ((1 << lj) < g_force_J) ++lj;
+            st.args.logJ = lj;
+            st.cfg.grid = (st.args.G + g_force_J - 1) / g_force_J;
+            st.args.ntiles = st.cfg.grid;
+            st.cfg.smem = cfg_smem_bytes(st.args.sub[0], st.dtype, g_force_J);
+            st.cfg.T = std::max(st.cfg.T, cfg_min_threads(st.args.sub[0], st.mode, g_force_J));
+        }
+        if (g_force_T && st.kind == 0) st.cfg.T = std::max(g_force_T, cfg_min_threads(st.args.sub[0], st.mode, st.cfg.J));
+        int e = 0;
+        switch (st.dtype) {
+            case KF_F32: e = run_step_t<float>(st); break;
+            case KF_F64: e = run_step_t<double>(st); break;
+            case KF_Q15: e = run_step_t<int16_t>(st); break;
+            case KF_Q31: e = run_step_t<int32_t>(st); break;
+        }
+        if (e) return e;
+    }
+    return 0;
+}
+
+extern "C" {
+
+void emu_force(int J, int T) {
+    g_force_J = J;
+    g_force_T = T;
+}
+
+int emu_c2c(int dtype, int n, int inverse, int lmax, const void* in, void* out, long long batch, long long in_dist,
+            long long in_stride, long long out_dist) {
+    Plan p;
+    if (!p.build(dtype, n, inverse, lmax)) return -2;
+    p.bind(p.blob.data());
+    Schedule s;
+    if (!schedule_c2c(p, batch, in_dist, in_stride, out_dist, s)) return -3;
+    return run_schedule(s, in, out);
+}
+
+int emu_r2c(int dtype, int nfft, int lmax, const void* in, void* out, long long batch) {
+    Plan p;
+    if (!p.build(dtype, nfft / 2, 0, lmax, nfft)) return -2;
+    p.bind(p.blob.data());
+    Schedule s;
+    if (!schedule_r2c(p, batch, nfft, nfft / 2 + 1, s)) return -3;
+    return run_schedule(s, in, out);
+}
+
+int emu_c2r(int dtype, int nfft, int lmax, const void* in, void* out, long long batch) {
+    Plan p;
+    if (!p.build(dtype, nfft / 2, 1, lmax, nfft)) return -2;
+    p.bind(p.blob.data());
+    Schedule s;
+    if (!schedule_c2r(p, batch, nfft / 2 + 1, nfft, s)) return -3;
+    return run_schedule(s, in, out);
+}
+
+// In-place complex transform along one axis of a row-major array.
+int emu_axis(int dtype, const int* dims, int ndims, int axis, int inverse, void* buf) {
+    Plan p;
+    if (!p.build(dtype, dims[axis], inverse)) return -2;
+    p.bind(p.blob.data());
+    Schedule s;
+    if (!schedule_axis(p, dims, ndims, axis, 1, 0, 1, s)) return -3;
+    return run_schedule(s, buf, buf);
+}
+
+// Real fast FIR with the library's block plan (H computed by the caller,
+// already scaled by 1/nfft).
+int emu_fastfir(const float* H, long long nfft, long long L, const float* x, long long Ns, float* y) {
+    Plan fw, iv;
+    if (!fw.build(KF_F32, (int)nfft / 2, 0, 0, (int)nfft)) return -2;
+    if (!iv.build(KF_F32, (int)nfft / 2, 1, 0, (int)nfft)) return -2;
+    fw.bind(fw.blob.data());
+    iv.bind(iv.blob.data());
+    Schedule s;
+    if (!schedule_fastfir(fw, iv, L, Ns, 0, s)) return -3;
+    return run_schedule(s, x, y, H);
+}
+
+int emu_plan_info(int dtype, int n, int lmax, int* out) {
+    Plan p;
+    if (!p.build(dtype, n, 0, lmax)) return -2;
+    out[0] = p.nsub;
+    out[1] = p.sub[0].L;
+    out[2] = p.nsub > 1 ? p.sub[1].L : 0;
+    out[3] = p.sub[0].npass;
+    return 0;
+}
+}
