@@ -1,0 +1,313 @@
+"""Benchmark of the GPU KISS FFT path on one GB300.
+
+Workload (default, "mixed-radix"): complex forward transforms at
+nfft in {480, 1000, 3003, 65536} -- the kf_factor plans [4,4,2,3,5],
+[4,2,5,5,5], [3,7,11,13] (generic radix) and [4]*8 (two HBM passes) -- each
+with a batch of 256 MiB of input, for float32, Q15 and Q31 samples
+(float inputs uniform[-1,1), fixed-point inputs uniform over the full
+integer range, seed 1; synthetic, generated on the host).  One step runs
+all 12 (type, size) batches once.  Every input batch is larger than the
+129 MB L2, so no L2 flush is needed between steps.
+
+Printed JSON line (one, on rank 0):
+  value   whole-job HBM throughput, GB/s of compulsory bytes
+          (2*N*sizeof(complex) per transform), inputs resident in HBM
+  e2e     the same through the drop-in C ABI with host (pinned) buffers,
+          host<->device copies inside the timed region
+  roofline  the dominant kernel's achieved GB/s (its compulsory bytes per
+          launch / its CUDA-event launch time) against the measured HBM peak
+  cpu_baseline  the CPU restatement of the reference path (oracle/, OpenMP
+          over transforms) on this host's cores, on a bounded sample
+
+--impl reference times that CPU path on the same workload instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+SIZES = [480, 1000, 3003, 65536]
+DTYPES = ["float", "int16_t", "int32_t"]
+ESZ = {"float": 8, "double": 16, "int16_t": 4, "int32_t": 8}
+BATCH_BYTES = 256 * 1024 * 1024
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+_CASES = None
+
+
+def units():
+    if _CASES:
+        return list(_CASES)
+    out = []
+    for dt in DTYPES:
+        for n in SIZES:
+            b = BATCH_BYTES // (n * ESZ[dt])
+            out.append((dt, n, b))
+    return out
+
+
+def make_input(dt, n, b, seed=1):
+    import inputs
+    return inputs.cpx((b, n), dt, seed + n)
+
+
+class ClockSampler(object):
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    import torch
+
+    import kissfft_gb300 as kf
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    us = units()
+    cfgs, xs, ys, host_in = [], [], [], []
+    for dt, n, b in us:
+        x = make_input(dt, n, b)
+        host_in.append(x)
+        xv = x.view(np.float32) if dt == "float" else x
+        xt = torch.from_numpy(np.ascontiguousarray(xv)).to(dev)
+        xs.append(xt)
+        ys.append(torch.empty_like(xt))
+        cfgs.append(kf.kiss_fft_alloc(n, 0, dt))
+    launches_per_unit = [kf.plan_info(c)[3] for c in cfgs]  # HBM passes = kernel launches
+    kf.set_specialize(args.specialize)
+    t_prep = time.perf_counter()
+    for c, (dt, n, b) in zip(cfgs, us):
+        kf.prepare(c, b)
+    t_prep = time.perf_counter() - t_prep
+
+    def step(events=None):
+        for i, (dt, n, b) in enumerate(us):
+            if events is not None:
+                events[i][0].record(stream)
+            kf.kiss_fft_batch(cfgs[i], xs[i], ys[i], b)
+            if events is not None:
+                events[i][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # timed region: whole steps, device time
+    clk = ClockSampler()
+    clk.start()
+    time.sleep(0.3)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for _ in range(args.steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    alg_bytes = sum(2 * n * ESZ[dt] * b for dt, n, b in us)
+    value = alg_bytes / (ms * 1e-3) / 1e9
+    # per-unit launch times (same workload, events between launches)
+    ev = [[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)] for _ in us]
+    per = [0.0] * len(us)
+    for _ in range(max(1, args.steps)):
+        step(ev)
+        torch.cuda.synchronize()
+        for i in range(len(us)):
+            per[i] += ev[i][0].elapsed_time(ev[i][1]) / max(1, args.steps)
+    unit_rows = []
+    for i, (dt, n, b) in enumerate(us):
+        byts = 2 * n * ESZ[dt] * b
+        unit_rows.append({"dtype": dt, "nfft": n, "batch": b, "ms": round(per[i], 4),
+                          "gbs": round(byts / (per[i] * 1e-3) / 1e9, 1), "launches": launches_per_unit[i]})
+    dom = max(range(len(us)), key=lambda i: per[i])
+    peak, peak_kind = peaks()
+    dt_, n_, b_ = us[dom]
+    dom_bytes = 2 * n_ * ESZ[dt_] * b_
+    achieved = dom_bytes / (per[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "kf_engine_kernel %s nfft=%d batch=%d (%d launch%s)" % (
+        dt_, n_, b_, launches_per_unit[dom], "es" if launches_per_unit[dom] > 1 else ""),
+        "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+        "frac": round(achieved / peak, 4), "traffic": args.traffic}
+    # e2e: host pinned buffers through the C ABI (H2D + D2H inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        hin = [torch.from_numpy(np.ascontiguousarray(x.view(np.float32) if dt == "float" else x)).pin_memory()
+               for x, (dt, n, b) in zip(host_in, us)]
+        hout = [torch.empty_like(h).pin_memory() for h in hin]
+        kf.kiss_fft_batch(cfgs[0], hin[0], hout[0], us[0][2])
+        e_steps = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        for _ in range(e_steps):
+            for i, (dt, n, b) in enumerate(us):
+                kf.kiss_fft_batch(cfgs[i], hin[i], hout[i], b)
+        torch.cuda.synchronize()
+        e_ms = (time.perf_counter() - ts) * 1e3 / e_steps
+        h2d = sum(h.numel() * h.element_size() for h in hin)
+        e2e = {"value": round(alg_bytes / (e_ms * 1e-3) / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": h2d, "ms_per_step": round(e_ms, 3)}
+        # the e2e output must equal the device-resident output
+        for i in range(len(us)):
+            if not torch.equal(hout[i], ys[i].cpu()):
+                raise RuntimeError("e2e output differs from device output for %s" % (us[i],))
+    return {"value": value, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": args.steps * sum(launches_per_unit), "alg_bytes": alg_bytes,
+            "prepare_s": round(t_prep, 2)}
+
+
+# ------------------------------------------------------------------ CPU arm
+def run_cpu_sample(frac, nthreads, repeat=1):
+    """The oracle (CPU restatement of the reference path) on a sample of each
+    batch; returns GB/s of compulsory bytes and the sample description."""
+    from oracle import kfo
+    tot_bytes, tot_s = 0, 0.0
+    for dt, n, b in units():
+        bs = max(1, int(b * frac))
+        x = make_input(dt, n, bs)
+        kfo.fft(x[:1], 0, dt, nthreads=1)
+        ts = time.perf_counter()
+        for _ in range(repeat):
+            kfo.fft(x, 0, dt, nthreads=nthreads)
+        tot_s += time.perf_counter() - ts
+        tot_bytes += 2 * n * ESZ[dt] * bs * repeat
+    return tot_bytes / tot_s / 1e9, tot_s
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-frac", type=float, default=1.0 / 64)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="dram bytes per launch of the dominant kernel from an ncu capture")
+    ap.add_argument("--specialize", type=int, default=1,
+                    help="1: plan-specialised kernels (compiled before warm-up); 0: precompiled family kernels")
+    ap.add_argument("--case", action="append", default=[],
+                    help="run only these units, TYPE:NFFT:BATCH (profiling runs)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.case:
+        global _CASES
+        _CASES = []
+        for c in args.case:
+            dt, n, b = c.split(":")
+            _CASES.append((dt, int(n), int(b)))
+        args.no_e2e = args.no_cpu = True
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    config = {"workload": "mixed-radix complex forward: nfft 480,1000,3003,65536 x float32,Q15,Q31, "
+                          "256 MiB input per batch", "sizes": SIZES, "dtypes": DTYPES,
+              "batches": [b for _, _, b in units()], "l2": "inputs larger than L2 (256 MiB per batch)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import kfo
+        nth = kfo.max_threads()
+        gbs, secs = run_cpu_sample(args.cpu_frac, nth)
+        for _ in range(args.warmup):
+            pass
+        per = []
+        for _ in range(args.steps):
+            g, s = run_cpu_sample(args.cpu_frac, nth)
+            per.append(g)
+        v = statistics.median(per)
+        sample = "1/%d of every batch per step (%d transforms)" % (round(1 / args.cpu_frac),
+                                                                   sum(max(1, int(b * args.cpu_frac))
+                                                                       for _, _, b in units()))
+        line = {"impl": "reference", "metric": "HBM GB/s (compulsory bytes), batched FFT", "value": round(v, 3),
+                "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
+                "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": nth, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    r = run_gpu(args)
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        from oracle import kfo
+        nth = kfo.max_threads()
+        g, secs = run_cpu_sample(args.cpu_frac, nth)
+        cpu = {"value": round(g, 3), "unit": "GB/s", "cores": nth, "kind": "port",
+               "sample": "1/%d of every batch (%.1f s of CPU work)" % (round(1 / args.cpu_frac), secs)}
+    if rank == 0:
+        line = {"metric": "HBM GB/s (compulsory bytes), batched FFT", "value": round(r["value"], 1), "unit": "GB/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms"], 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
+                "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
+                "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
+                "kernels": "plan-specialised (NVRTC, compiled before warm-up in %.1f s)" % r["prepare_s"]
+                if args.specialize else "precompiled families"}
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

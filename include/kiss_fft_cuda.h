@@ -150,6 +150,11 @@ const char *kiss_fft_cuda_last_error(void);
  * status of kissfft_gb300.h (the void calls report failures only on stderr,
  * as the reference does) */
 int kiss_fft_cuda_status(void);
+/* Plan-specialised kernels (kissfft_gb300.h: kfg_set_specialize) and their
+ * ahead-of-time preparation for a batch size (kfg_plan_prepare; batch is
+ * the signal length for a fast FIR cfg). */
+int kiss_fft_cuda_set_specialize(int on);
+int kiss_fft_cuda_prepare(void *cfg, long long batch);
 
 #ifdef __cplusplus
 }

@@ -80,6 +80,21 @@ int kfg_synchronize(void);
 const char *kfg_last_error(void);
 int kfg_next_fast_size(int n);
 
+/* Plan-specialised kernels.  With specialisation on, every launch uses a
+ * kernel compiled for its exact plan shape (all strides and radices
+ * constant), compiled at run time with NVRTC on first use and cached on
+ * disk (KISSFFT_GB300_CACHE); without it the precompiled kernels that read
+ * the shape at run time are used.  Default off; KISSFFT_GB300_SPECIALIZE=1
+ * turns it on. */
+int kfg_set_specialize(int on);
+/* Compile (or load) the specialised kernels a batched call of this shape
+ * will use, so that the compile cost is paid here.  For a fast FIR plan,
+ * batch is the signal length. */
+int kfg_plan_prepare(kfg_plan *p, long long batch, long long in_dist, long long out_dist);
+/* Compile, without loading or a GPU, the specialised kernels of a complex
+ * (real = 0) or real (real = 1) plan: a check of the embedded sources. */
+int kfg_specialize_check(int dtype, int real, int n, int inverse, long long batch);
+
 /* Plan introspection for tests and tools: out[0] = transform kind, out[1] =
  * dtype, out[2] = length, out[3] = number of HBM passes of a 1-D plan,
  * out[4] = kernel family, out[5] = tile length. */

@@ -105,6 +105,7 @@ def load(dtype="float"):
         L.kiss_fastfir_cuda_filter.restype = sz
         L.kiss_fastfir_cuda_filter.argtypes = [vp, vp, sz, vp]
         L.kiss_fft_cuda_set_stream.argtypes = [vp]
+        L.kiss_fft_cuda_prepare.argtypes = [vp, ll]
         L.kiss_fft_cuda_last_error.restype = ctypes.c_char_p
         _libs[dtype] = L
     return _libs[dtype]
@@ -339,6 +340,19 @@ def kiss_fastfir_filter(cfg, x, y):
     return int(n)
 
 
+# ---------------------------------------------------------------- specialised kernels
+def set_specialize(on=True):
+    """Use kernels compiled (NVRTC, cached on disk) for each plan's exact shape."""
+    core().kfg_set_specialize(int(bool(on)))
+
+
+def prepare(cfg, batch):
+    """Compile the specialised kernels a batched call on cfg will use."""
+    rc = cfg.lib.kiss_fft_cuda_prepare(ctypes.c_void_p(cfg.ptr), int(batch))
+    if rc:
+        _raise_on_status(cfg.lib, "prepare")
+
+
 # ---------------------------------------------------------------- misc
 def last_error(dtype="float"):
     msg = load(dtype).kiss_fft_cuda_last_error()
@@ -347,7 +361,6 @@ def last_error(dtype="float"):
 
 def plan_info(cfg):
     """(kind, dtype, length, hbm_passes, family, tile) of a cfg's device plan."""
-    import numpy as np
     c = core()
     out = (ctypes.c_int * 6)()
     # the cfg's first field after the header is the core plan pointer

@@ -39,7 +39,28 @@ DROPIN_DEFS = {
     "int16_t": ["-DKF_DROPIN_DTYPE=2", "-DFIXED_POINT=16"],
     "int32_t": ["-DKF_DROPIN_DTYPE=3", "-DFIXED_POINT=32"],
 }
-HEADERS = ["kf_arith.cuh", "kf_desc.h", "kf_engine.cuh", "kf_runner.cuh", "kf_kernels.cuh", "kf_plan.h"]
+HEADERS = ["kf_arith.cuh", "kf_desc.h", "kf_engine.cuh", "kf_runner.cuh", "kf_kernels.cuh", "kf_plan.h",
+           "kf_shape.h", "kf_stdint.h", "kf_device.cuh", "kf_spec.cuh"]
+# the device headers NVRTC compiles specialised kernels from (embedded in the core library)
+JIT_HEADERS = ["kf_spec.cuh", "kf_device.cuh", "kf_runner.cuh", "kf_engine.cuh", "kf_arith.cuh", "kf_desc.h",
+               "kf_shape.h", "kf_stdint.h"]
+
+
+def _gen_headers_cpp(out):
+    parts = ["// generated by kissfft_gb300/build.py: device headers for NVRTC", "namespace kf {",
+             "extern const int kf_hdr_count = %d;" % len(JIT_HEADERS),
+             "extern const char* const kf_hdr_names[] = {%s};" % ", ".join('"%s"' % h for h in JIT_HEADERS),
+             "extern const char* const kf_hdr_srcs[] = {"]
+    for h in JIT_HEADERS:
+        with open(os.path.join(CSRC, h)) as f:
+            txt = f.read()
+        chunks = [txt[i:i + 12000] for i in range(0, len(txt), 12000)]
+        parts.append("    " + " ".join('R"KFHDR(%s)KFHDR"' % c for c in chunks) + ",")
+    parts += ["};", "}  // namespace kf", ""]
+    data = "\n".join(parts)
+    if not (os.path.exists(out) and open(out).read() == data):
+        with open(out, "w") as f:
+            f.write(data)
 
 
 def core_lib():
@@ -98,13 +119,20 @@ def build(verbose=False, jobs=None):
     out = os.path.join(BUILD, "kf_plan.o")
     tasks.append((["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "kf_plan.cpp"), "-o", out],
                   [os.path.join(CSRC, "kf_plan.cpp")] + hdrs, out))
+    out = os.path.join(BUILD, "kf_jit.o")
+    tasks.append((["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "kf_jit.cpp"), "-o", out],
+                  [os.path.join(CSRC, "kf_jit.cpp")] + hdrs, out))
+    gen = os.path.join(BUILD, "kf_hdrs_gen.cpp")
+    _gen_headers_cpp(gen)
+    out = os.path.join(BUILD, "kf_hdrs_gen.o")
+    tasks.append((["g++"] + CXXFLAGS + ["-c", gen, "-o", out], [gen], out))
     jobs = jobs or max(1, os.cpu_count() or 1)
     # longest first: the general-family units
     tasks.sort(key=lambda t: 0 if "_2.o" in t[2] else 1)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda t: _compile(t[0], t[1], t[2], verbose), tasks))
     core = core_lib()
-    link = [NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", core] + objs
+    link = [NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", core] + objs + ["-lnvrtc"]
     _compile(link, objs, core, verbose)
     for dt in DTYPES:
         out = dropin_lib(dt)

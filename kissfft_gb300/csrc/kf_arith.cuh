@@ -13,9 +13,9 @@
 // same operands as kf_bfly2/3/4/5/generic (kiss_fft.c:15-233), so Q15/Q31
 // results are bit-identical to the reference.
 #pragma once
-#include <stdint.h>
+#include "kf_stdint.h"
 
-#if defined(__CUDACC__)
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
 #define KF_HD __host__ __device__ __forceinline__
 #else
 #define KF_HD inline

@@ -15,7 +15,7 @@
 //   pass         one or two consecutive stages of a sub-plan executed on a
 //                register tile (group) of R = p_a[*p_b] elements.
 #pragma once
-#include <stdint.h>
+#include "kf_stdint.h"
 
 #define KF_MAXST 32
 #define KF_MAXJ 64
@@ -49,22 +49,31 @@ struct KPass {
     int H;        // groups along the higher digits  (= iloc of stage a)
     int ML;       // groups along the lower digits   (= mloc of stage a+ns-1)
     int rev_off;  // digit-reversal table of the lower digits (-1 if ML == 1)
+    int pad;
+    unsigned long long hdiv;  // magic for n / H   (fdiv)
+    unsigned long long gdiv;  // magic for n / (H*ML)
 };
 
+// Shape of a sub-plan: integers only, so that a whole shape can also be a
+// compile-time constant of a specialised kernel.
 struct KSub {
-    int N;        // full transform length (generic twiddle modulus)
-    int L;        // sub-plan length
+    int N;            // full transform length (generic twiddle modulus)
+    int L;            // sub-plan length
     int nst, npass;
-    int m_low;    // global span of the last stage in the range (1 for the leaf range)
+    int m_low;        // global span of the last stage in the range (1 for the leaf range)
     int inverse;
-    int pad0, pad1;
+    int revfull_off;  // position -> input-order table (L ints) in the reverse tables, or -1
+    int pad;
+    KStage st[KF_MAXST];
+    KPass ps[KF_MAXST];
+};
+
+// Device tables of a plan.
+struct KTab {
     const void* tw_full;   // N twiddles (plan dtype)
     const void* tw_stage;  // compact per-stage tables
     const int* rev;        // digit-reversal tables
-    const int* revfull;    // local position -> local input order (L entries) or null
     const void* super_tw;  // real-transform super twiddles (ncfft/2) or null
-    KStage st[KF_MAXST];
-    KPass ps[KF_MAXST];
 };
 
 // One launch: G jobs (sub-transforms), J per CTA tile.  Job jg decomposes as
@@ -73,6 +82,7 @@ struct KSub {
 // (units: complex elements, or real samples for the real-input modes).
 struct KArgs {
     KSub sub[2];              // sub[1]: inverse plan of the fast FIR
+    KTab tab[2];
     const void* in;
     void* out;
     const void* fir_H;        // fast FIR frequency response (nfft/2+1 bins)

@@ -368,4 +368,18 @@ const char* kiss_fft_cuda_last_error(void) { return kfg_last_error(); }
 
 int kiss_fft_cuda_status(void) { return t_status; }
 
+int kiss_fft_cuda_set_specialize(int on) { return kfg_set_specialize(on); }
+
+int kiss_fft_cuda_prepare(void* cfg, long long batch) {
+    t_status = 0;
+    kiss_fft_cuda_state* s = (kiss_fft_cuda_state*)cfg;
+    if (!s || s->magic != kMagic || !s->plan) {
+        report("kiss_fft_cuda_prepare", "invalid cfg");
+        return KFG_EINVAL;
+    }
+    int rc = note(kfg_plan_prepare(s->plan, batch, 0, 0));
+    if (rc != KFG_OK) report_last("kiss_fft_cuda_prepare");
+    return rc;
+}
+
 }  // extern "C"

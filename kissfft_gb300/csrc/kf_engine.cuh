@@ -11,47 +11,108 @@
 // memory at index I = A*sA + job*sJ (A = input-order index), XOR-swizzled
 // so that both the input-order and the position-order sweeps are
 // bank-conflict free for power-of-two strides.
+//
+// Every function takes the sub-plan shape (KSub, integers only) and its
+// device tables (KTab) separately: a specialised kernel passes a
+// compile-time constant shape and the compiler folds every stride.
 #pragma once
+
 #include "kf_arith.cuh"
 #include "kf_desc.h"
-#include <string.h>
+#include "kf_shape.h"
+
+#if !defined(__CUDACC__) && !defined(__CUDACC_RTC__)
+// host compilers (the CPU emulator): the CUDA vector types used below
+struct uint2 {
+    unsigned x, y;
+};
+struct alignas(16) uint4 {
+    unsigned x, y, z, w;
+};
+#endif
 
 namespace kf {
 
-// Read-only (non-coherent cache) load of tables: twiddles, reverse tables.
+// Read-only (non-coherent cache) loads of tables: twiddles, reverse
+// tables.  The raw words go through aligned unions (no memcpy: NVRTC has no
+// C library).
+template <typename T, typename V>
+union KfPun {
+    V v;
+    T t;
+};
+
 template <typename T>
 KF_HD T ldro(const T* p) {
 #if defined(__CUDA_ARCH__)
-    T r;
     if constexpr (sizeof(T) == 4) {
-        unsigned v = __ldg((const unsigned*)p);
-        memcpy(&r, &v, 4);
+        KfPun<T, unsigned> u;
+        u.v = __ldg((const unsigned*)p);
+        return u.t;
     } else if constexpr (sizeof(T) == 8) {
-        uint2 v = __ldg((const uint2*)p);
-        memcpy(&r, &v, 8);
+        KfPun<T, uint2> u;
+        u.v = __ldg((const uint2*)p);
+        return u.t;
     } else if constexpr (sizeof(T) == 16) {
-        uint4 v = __ldg((const uint4*)p);
-        memcpy(&r, &v, 16);
+        KfPun<T, uint4> u;
+        u.v = __ldg((const uint4*)p);
+        return u.t;
     } else {
-        r = *p;
+        return *p;
     }
-    return r;
 #else
     return *p;
 #endif
 }
 #define KF_LDG(p) ::kf::ldro(p)
 
+template <typename S, int W>
+struct KfVec {
+    static constexpr int bytes = W * (int)sizeof(cpx<S>);
+    static constexpr int nu = bytes >= 16 ? bytes / 16 : 1;
+    union U {
+        uint4 q[nu];
+        uint2 d;
+        unsigned w;
+        cpx<S> c[W];
+    };
+};
+
+// W consecutive complex table entries; the caller guarantees alignment to
+// min(16, W*sizeof(cpx)) bytes.
+template <typename S, int W>
+KF_HD void ldro_vec(const cpx<S>* p, cpx<S>* out) {
+#if defined(__CUDA_ARCH__)
+    typename KfVec<S, W>::U u;
+    constexpr int bytes = KfVec<S, W>::bytes;
+    if constexpr (bytes >= 16) {
+#pragma unroll
+        for (int i = 0; i < bytes / 16; ++i) u.q[i] = __ldg((const uint4*)p + i);
+    } else if constexpr (bytes == 8) {
+        u.d = __ldg((const uint2*)p);
+    } else {
+        u.w = __ldg((const unsigned*)p);
+    }
+#pragma unroll
+    for (int i = 0; i < W; ++i) out[i] = u.c[i];
+#else
+    for (int i = 0; i < W; ++i) out[i] = p[i];
+#endif
+}
+
+// n / d for n * d < 2^40 with M = div_magic(d)
+KF_HD int fdiv(int n, unsigned long long M) { return (int)(((unsigned long long)(unsigned)n * M) >> 40); }
+
 template <typename S>
 struct SwzBits {
-    static const int v = sizeof(cpx<S>) == 4 ? 5 : (sizeof(cpx<S>) == 8 ? 4 : 3);
+    static constexpr int v = sizeof(cpx<S>) == 4 ? 5 : (sizeof(cpx<S>) == 8 ? 4 : 3);
 };
 
 // XOR-fold swizzle inside aligned blocks of 2^B elements (a bijection).
 template <typename S>
 KF_HD int swz(int I) {
-    const int B = SwzBits<S>::v;
-    const int f = (I >> B) ^ (I >> (2 * B)) ^ (I >> (3 * B)) ^ (I >> (4 * B));
+    constexpr int B = SwzBits<S>::v;
+    const int f = (I >> B) ^ (I >> (2 * B)) ^ (I >> (3 * B));
     return I ^ (f & ((1 << B) - 1));
 }
 
@@ -63,14 +124,14 @@ struct Tile {
     int sA, sJ;  // shared index strides of the input-order index and of the job
     int J, logJ, col;
     int T;       // threads working on the tile
+    int in_stride, out_stride;
     const long long* inb;
     const long long* outb;
     const int* U;
-    const long long* lim_in;   // real-input limit (fast FIR); null otherwise
+    const long long* lim_in;   // real-input limit (fast FIR)
     const long long* lim_out;  // real-output limit (fast FIR)
     const void* in;
     void* out;
-    long long in_stride, out_stride;
     int* err;
 
     KF_HD int sidx(int A, int job) const { return swz<S>(A * sA + job * sJ); }
@@ -80,33 +141,74 @@ struct Tile {
 };
 
 // ------------------------------------------------------------ global access
-// Complex load/store; MODE_FIR moves real samples with limits instead.
+// A group's HBM base: element k sits at base + off_k * stride.  MODE_FIR
+// moves real samples with limits (zero padding on input) instead.
 template <typename S, int MODE>
-KF_HD cpx<S> gload(const Tile<S>& t, int job, int A) {
-    cpx<S> v;
-    if constexpr (MODE == MODE_FIR) {
-        const S* x = (const S*)t.in + t.inb[job];
-        long long i0 = 2LL * A;
-        long long lim = t.lim_in[job];
-        v.r = i0 < lim ? x[i0] : (S)0;
-        v.i = i0 + 1 < lim ? x[i0 + 1] : (S)0;
-    } else {
-        v = ((const cpx<S>*)t.in)[t.inb[job] + (long long)A * t.in_stride];
+struct GIn {
+    const cpx<S>* p;
+    const S* r;
+    long long lim;
+    int stride;
+    KF_HD cpx<S> ld(int off) const {
+        cpx<S> v;
+        if constexpr (MODE == MODE_FIR) {
+            const long long i0 = 2LL * off;
+            v.r = i0 < lim ? r[i0] : (S)0;
+            v.i = i0 + 1 < lim ? r[i0 + 1] : (S)0;
+        } else {
+            v = p[(long long)(off * stride)];
+        }
+        return v;
     }
-    return v;
+};
+
+template <typename S, int MODE>
+KF_HD GIn<S, MODE> gin(const Tile<S>& t, int job, int A0) {
+    GIn<S, MODE> g;
+    g.stride = t.in_stride;
+    if constexpr (MODE == MODE_FIR) {
+        g.r = (const S*)t.in + t.inb[job] + 2LL * A0;
+        g.lim = t.lim_in[job] - 2LL * A0;
+        g.p = nullptr;
+    } else {
+        g.p = (const cpx<S>*)t.in + t.inb[job] + (long long)A0 * t.in_stride;
+        g.r = nullptr;
+        g.lim = 0;
+    }
+    return g;
 }
 
 template <typename S, int MODE>
-KF_HD void gstore(const Tile<S>& t, int job, int pos, cpx<S> v) {
-    if constexpr (MODE == MODE_FIR) {
-        S* y = (S*)t.out + t.outb[job];
-        long long i0 = 2LL * pos;
-        long long lim = t.lim_out[job];
-        if (i0 < lim) y[i0] = v.r;
-        if (i0 + 1 < lim) y[i0 + 1] = v.i;
-    } else {
-        ((cpx<S>*)t.out)[t.outb[job] + (long long)pos * t.out_stride] = v;
+struct GOut {
+    cpx<S>* p;
+    S* r;
+    long long lim;
+    int stride;
+    KF_HD void st(int off, cpx<S> v) const {
+        if constexpr (MODE == MODE_FIR) {
+            const long long i0 = 2LL * off;
+            if (i0 < lim) r[i0] = v.r;
+            if (i0 + 1 < lim) r[i0 + 1] = v.i;
+        } else {
+            p[(long long)(off * stride)] = v;
+        }
     }
+};
+
+template <typename S, int MODE>
+KF_HD GOut<S, MODE> gout(const Tile<S>& t, int job, int pos0) {
+    GOut<S, MODE> g;
+    g.stride = t.out_stride;
+    if constexpr (MODE == MODE_FIR) {
+        g.r = (S*)t.out + t.outb[job] + 2LL * pos0;
+        g.lim = t.lim_out[job] - 2LL * pos0;
+        g.p = nullptr;
+    } else {
+        g.p = (cpx<S>*)t.out + t.outb[job] + (long long)pos0 * t.out_stride;
+        g.r = nullptr;
+        g.lim = 0;
+    }
+    return g;
 }
 
 // ------------------------------------------------------------ group decode
@@ -119,9 +221,8 @@ struct GroupIx {
 // Non-last passes enumerate the lower digits in input order (conflict-free
 // shared sweeps); the last pass enumerates them in position order
 // (coalesced output) and uses the reverse table.
-KF_HD GroupIx decode(const KPass& ps, const KSub& sb, int J, int logJ, int col, bool is_last, int gidx) {
+KF_HD GroupIx decode(const KPass& ps, const KTab& tb, int J, int logJ, int col, bool is_last, int gidx) {
     GroupIx g;
-    int gp = ps.H * ps.ML;
     int r;
     if (col) {
         g.job = gidx & (J - 1);
@@ -130,18 +231,18 @@ KF_HD GroupIx decode(const KPass& ps, const KSub& sb, int J, int logJ, int col, 
         g.job = 0;
         r = gidx;
     } else {
-        g.job = gidx / gp;
-        r = gidx - g.job * gp;
+        g.job = fdiv(gidx, ps.gdiv);
+        r = gidx - g.job * (ps.H * ps.ML);
     }
     int h, ulp, ul;
     if (is_last) {
         h = 0;
         ul = r;
-        ulp = ps.ML > 1 ? KF_LDG(sb.rev + ps.rev_off + ul) : 0;
+        ulp = ps.ML > 1 ? KF_LDG(tb.rev + ps.rev_off + ul) : 0;
     } else {
-        h = r % ps.H;
-        ulp = r / ps.H;
-        ul = ps.ML > 1 ? KF_LDG(sb.rev + ps.rev_off + ulp) : 0;
+        ulp = ps.H > 1 ? fdiv(r, ps.hdiv) : r;
+        h = r - ulp * ps.H;
+        ul = ps.ML > 1 ? KF_LDG(tb.rev + ps.rev_off + ulp) : 0;
     }
     g.A0 = h + ulp * ps.H * ps.R;
     g.pos0 = ul;
@@ -150,97 +251,116 @@ KF_HD GroupIx decode(const KPass& ps, const KSub& sb, int J, int logJ, int col, 
 }
 
 template <typename S, int P>
-KF_HD void stage_tw(const KSub& sb, const KStage& st, int u, cpx<S>* w, cpx<S>& c0, cpx<S>& c1) {
-    const cpx<S>* tws = (const cpx<S>*)sb.tw_stage + st.tw_off;
+KF_HD void stage_tw(const KTab& tb, const KStage& st, int u, cpx<S>* w, cpx<S>& c0, cpx<S>& c1) {
+    constexpr int W = P == 2 ? 1 : (P == 3 ? 2 : 4);
+    const cpx<S>* tws = (const cpx<S>*)tb.tw_stage + st.tw_off;
+    cpx<S> v[W];
+    ldro_vec<S, W>(tws + u * W, v);
 #pragma unroll
-    for (int q = 1; q < P; ++q) w[q - 1] = KF_LDG(tws + (q - 1) * st.m + u);
-    if constexpr (P == 3 || P == 5) c0 = KF_LDG(tws + (P - 1) * st.m);
-    if constexpr (P == 5) c1 = KF_LDG(tws + (P - 1) * st.m + 1);
+    for (int q = 1; q < P; ++q) w[q - 1] = v[q - 1];
+    if constexpr (P == 3 || P == 5) c0 = KF_LDG(tws + W * st.m);
+    if constexpr (P == 5) c1 = KF_LDG(tws + W * st.m + 1);
 }
 
 // ------------------------------------------------------------ group kernels
 // One stage of radix P (2..5) on a group of P elements.
 template <typename S, int MODE, int P>
-KF_HD void group1(const Tile<S>& t, const KSub& sb, const KPass& ps, const GroupIx& g, int U, bool src_g,
-                  bool dst_g) {
+KF_HD void group1(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, const GroupIx& g, int U,
+                  bool src_g, bool dst_g) {
     typedef cpx<S> C;
     const KStage& sa = sb.st[ps.a];
     C x[P];
+    if (src_g) {
+        const GIn<S, MODE> gi = gin<S, MODE>(t, g.job, g.A0);
 #pragma unroll
-    for (int q = 0; q < P; ++q) {
-        int A = g.A0 + q * sa.iloc;
-        x[q] = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
+        for (int q = 0; q < P; ++q) x[q] = gi.ld(q * sa.iloc);
+    } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q) x[q] = t.sld(g.A0 + q * sa.iloc, g.job);
     }
     C w[P > 1 ? P - 1 : 1], c0, c1;
-    stage_tw<S, P>(sb, sa, g.ul * sb.m_low + U, w, c0, c1);
+    stage_tw<S, P>(tb, sa, g.ul * sb.m_low + U, w, c0, c1);
     bfly<S, P, 1>(x, w, c0, c1, sb.inverse != 0);
+    if (dst_g) {
+        const GOut<S, MODE> go = gout<S, MODE>(t, g.job, g.pos0);
 #pragma unroll
-    for (int q = 0; q < P; ++q) {
-        if (dst_g)
-            gstore<S, MODE>(t, g.job, g.pos0 + q * sa.mloc, x[q]);
-        else
-            t.sst(g.A0 + q * sa.iloc, g.job, x[q]);
+        for (int q = 0; q < P; ++q) go.st(q * sa.mloc, x[q]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q) t.sst(g.A0 + q * sa.iloc, g.job, x[q]);
     }
 }
 
 // Two stages: stage a+1 (radix PB) then stage a (radix PA), element
 // (ea, eb) at register k = ea + PA*eb.
 template <typename S, int MODE, int PA, int PB>
-KF_HD void group2(const Tile<S>& t, const KSub& sb, const KPass& ps, const GroupIx& g, int U, bool src_g,
-                  bool dst_g) {
+KF_HD void group2(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, const GroupIx& g, int U,
+                  bool src_g, bool dst_g) {
     typedef cpx<S> C;
     const KStage& sa = sb.st[ps.a];
     const KStage& sbb = sb.st[ps.a + 1];
     C x[PA * PB];
+    if (src_g) {
+        const GIn<S, MODE> gi = gin<S, MODE>(t, g.job, g.A0);
 #pragma unroll
-    for (int eb = 0; eb < PB; ++eb)
+        for (int eb = 0; eb < PB; ++eb)
 #pragma unroll
-        for (int ea = 0; ea < PA; ++ea) {
-            int A = g.A0 + ea * sa.iloc + eb * sbb.iloc;
-            x[ea + PA * eb] = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
-        }
+            for (int ea = 0; ea < PA; ++ea) x[ea + PA * eb] = gi.ld(ea * sa.iloc + eb * sbb.iloc);
+    } else {
+#pragma unroll
+        for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+            for (int ea = 0; ea < PA; ++ea) x[ea + PA * eb] = t.sld(g.A0 + ea * sa.iloc + eb * sbb.iloc, g.job);
+    }
     {
         C w[PB - 1], c0, c1;
-        stage_tw<S, PB>(sb, sbb, g.ul * sb.m_low + U, w, c0, c1);
+        stage_tw<S, PB>(tb, sbb, g.ul * sb.m_low + U, w, c0, c1);
 #pragma unroll
         for (int ea = 0; ea < PA; ++ea) bfly<S, PB, PA>(x + ea, w, c0, c1, sb.inverse != 0);
     }
 #pragma unroll
     for (int eb = 0; eb < PB; ++eb) {
         C w[PA - 1], c0, c1;
-        stage_tw<S, PA>(sb, sa, (eb * sbb.mloc + g.ul) * sb.m_low + U, w, c0, c1);
+        stage_tw<S, PA>(tb, sa, (eb * sbb.mloc + g.ul) * sb.m_low + U, w, c0, c1);
         bfly<S, PA, 1>(x + PA * eb, w, c0, c1, sb.inverse != 0);
     }
+    if (dst_g) {
+        const GOut<S, MODE> go = gout<S, MODE>(t, g.job, g.pos0);
 #pragma unroll
-    for (int eb = 0; eb < PB; ++eb)
+        for (int eb = 0; eb < PB; ++eb)
 #pragma unroll
-        for (int ea = 0; ea < PA; ++ea) {
-            if (dst_g)
-                gstore<S, MODE>(t, g.job, g.pos0 + ea * sa.mloc + eb * sbb.mloc, x[ea + PA * eb]);
-            else
-                t.sst(g.A0 + ea * sa.iloc + eb * sbb.iloc, g.job, x[ea + PA * eb]);
-        }
+            for (int ea = 0; ea < PA; ++ea) go.st(ea * sa.mloc + eb * sbb.mloc, x[ea + PA * eb]);
+    } else {
+#pragma unroll
+        for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+            for (int ea = 0; ea < PA; ++ea) t.sst(g.A0 + ea * sa.iloc + eb * sbb.iloc, g.job, x[ea + PA * eb]);
+    }
 }
 
 // Generic radix P (a prime 7..31) on registers, kf_bfly_generic
 // (kiss_fft.c:192-233): output leg q1 sums legs q = 0..P-1 in order with
 // twiddle index (q*fstride*k) mod N, k = u + q1*m.
 template <typename S, int MODE, int P>
-KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KPass& ps, const GroupIx& g, int U, bool src_g,
-                  bool dst_g) {
+KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, const GroupIx& g, int U,
+                  bool src_g, bool dst_g) {
     typedef cpx<S> C;
     typedef Ar<S> Arr;
     const KStage& sa = sb.st[ps.a];
-    const C* tw = (const C*)sb.tw_full;
+    const C* tw = (const C*)tb.tw_full;
     C x[P];
+    if (src_g) {
+        const GIn<S, MODE> gi = gin<S, MODE>(t, g.job, g.A0);
 #pragma unroll
-    for (int q = 0; q < P; ++q) {
-        int A = g.A0 + q * sa.iloc;
-        C v = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
-        x[q] = Arr::template fixdiv<P>(v);
+        for (int q = 0; q < P; ++q) x[q] = Arr::template fixdiv<P>(gi.ld(q * sa.iloc));
+    } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q) x[q] = Arr::template fixdiv<P>(t.sld(g.A0 + q * sa.iloc, g.job));
     }
     const int u = g.ul * sb.m_low + U;
     const int N = sb.N;
+    GOut<S, MODE> go{};
+    if (dst_g) go = gout<S, MODE>(t, g.job, g.pos0);
 #pragma unroll 1
     for (int q1 = 0; q1 < P; ++q1) {
         const int step = sa.fs * (u + q1 * sa.m);
@@ -253,7 +373,7 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KPass& ps, const Group
             acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
         }
         if (dst_g)
-            gstore<S, MODE>(t, g.job, g.pos0 + q1 * sa.mloc, acc);
+            go.st(q1 * sa.mloc, acc);
         else
             t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
     }
@@ -263,29 +383,30 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KPass& ps, const Group
 // KF_MAXO outputs into registers (reading all p legs of each), then -- after
 // a barrier the caller places -- stores them.
 template <typename S, int MODE>
-KF_HD void rtg_compute(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_last, int tid, int T,
-                       bool src_g, cpx<S>* outv) {
+KF_HD void rtg_compute(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool is_last, int tid,
+                       int T, bool src_g, cpx<S>* outv) {
     typedef cpx<S> C;
     typedef Ar<S> Arr;
     const KStage& sa = sb.st[ps.a];
-    const C* tw = (const C*)sb.tw_full;
+    const C* tw = (const C*)tb.tw_full;
     const int p = sa.p, N = sb.N;
     const int NG = t.J * ps.H * ps.ML;
 #pragma unroll
     for (int i = 0; i < KF_MAXO; ++i) {
-        int o = tid + i * T;
+        const int o = tid + i * T;
         if (o >= NG * p) break;
-        int q1 = o / NG, gidx = o - q1 * NG;
-        GroupIx g = decode(ps, sb, t.J, t.logJ, t.col, is_last, gidx);
+        const int q1 = o / NG, gidx = o - q1 * NG;
+        const GroupIx g = decode(ps, tb, t.J, t.logJ, t.col, is_last, gidx);
         if (!t.valid(g.job)) continue;
-        int U = t.U[g.job];
+        const int U = t.U[g.job];
         const int step = sa.fs * (g.ul * sb.m_low + U + q1 * sa.m);
         int twidx = 0;
-        C v0 = src_g ? gload<S, MODE>(t, g.job, g.A0) : t.sld(g.A0, g.job);
+        GIn<S, MODE> gi{};
+        if (src_g) gi = gin<S, MODE>(t, g.job, g.A0);
+        C v0 = src_g ? gi.ld(0) : t.sld(g.A0, g.job);
         C acc = Arr::fixdiv_rt(v0, p);
         for (int q = 1; q < p; ++q) {
-            int A = g.A0 + q * sa.iloc;
-            C v = src_g ? gload<S, MODE>(t, g.job, A) : t.sld(A, g.job);
+            C v = src_g ? gi.ld(q * sa.iloc) : t.sld(g.A0 + q * sa.iloc, g.job);
             twidx += step;
             if (twidx >= N) twidx -= N;
             acc = c_add(acc, Arr::cmul(Arr::fixdiv_rt(v, p), KF_LDG(tw + twidx)));
@@ -295,59 +416,56 @@ KF_HD void rtg_compute(const Tile<S>& t, const KSub& sb, const KPass& ps, bool i
 }
 
 template <typename S, int MODE>
-KF_HD void rtg_store(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_last, int tid, int T, bool dst_g,
-                     const cpx<S>* outv) {
+KF_HD void rtg_store(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool is_last, int tid,
+                     int T, bool dst_g, const cpx<S>* outv) {
     const KStage& sa = sb.st[ps.a];
     const int p = sa.p;
     const int NG = t.J * ps.H * ps.ML;
 #pragma unroll
     for (int i = 0; i < KF_MAXO; ++i) {
-        int o = tid + i * T;
+        const int o = tid + i * T;
         if (o >= NG * p) break;
-        int q1 = o / NG, gidx = o - q1 * NG;
-        GroupIx g = decode(ps, sb, t.J, t.logJ, t.col, is_last, gidx);
+        const int q1 = o / NG, gidx = o - q1 * NG;
+        const GroupIx g = decode(ps, tb, t.J, t.logJ, t.col, is_last, gidx);
         if (!t.valid(g.job)) continue;
         if (dst_g)
-            gstore<S, MODE>(t, g.job, g.pos0 + q1 * sa.mloc, outv[i]);
+            gout<S, MODE>(t, g.job, g.pos0).st(q1 * sa.mloc, outv[i]);
         else
             t.sst(g.A0 + q1 * sa.iloc, g.job, outv[i]);
     }
 }
 
-// All groups of one (non runtime-generic) pass handled by thread tid.
-// FAM limits the pass kinds compiled in: kf_factor emits 4s, at most one 2,
-// then 3s, 5s and larger primes, so only 9 ordered radix pairs can occur.
-template <typename S, int MODE, int FAM>
-KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_last, int tid, int T, bool src_g,
-                    bool dst_g) {
+// All groups of one (non runtime-generic) pass handled by thread tid.  KM
+// is the mask of pass kinds compiled in (kind_bit): a family kernel covers
+// a family of plans, a specialised kernel exactly its own passes.  kf_factor
+// emits 4s, at most one 2, then 3s, 5s and larger primes, so only 9 ordered
+// radix pairs can occur.
+template <typename S, int MODE, unsigned KM>
+KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool is_last, int tid, int T,
+                    bool src_g, bool dst_g) {
     const int NG = t.J * ps.H * ps.ML;
     for (int gidx = tid; gidx < NG; gidx += T) {
-        GroupIx g = decode(ps, sb, t.J, t.logJ, t.col, is_last, gidx);
+        const GroupIx g = decode(ps, tb, t.J, t.logJ, t.col, is_last, gidx);
         if (!t.valid(g.job)) continue;
         const int U = t.U[g.job];
         switch (ps.kind) {
-#define KF_G1(P) \
-    case P: group1<S, MODE, P>(t, sb, ps, g, U, src_g, dst_g); break;
-#define KF_G2(PA, PB) \
-    case 10 * PA + PB: group2<S, MODE, PA, PB>(t, sb, ps, g, U, src_g, dst_g); break;
-#define KF_GG(P) \
-    case 100 + P: groupg<S, MODE, P>(t, sb, ps, g, U, src_g, dst_g); break;
+#define KF_G1(P)                                                                            \
+    case P:                                                                                 \
+        if constexpr ((KM & kind_bit(P)) != 0) group1<S, MODE, P>(t, sb, tb, ps, g, U, src_g, dst_g); \
+        break;
+#define KF_G2(PA, PB)                                                                       \
+    case 10 * PA + PB:                                                                      \
+        if constexpr ((KM & kind_bit(10 * PA + PB)) != 0)                                   \
+            group2<S, MODE, PA, PB>(t, sb, tb, ps, g, U, src_g, dst_g);                     \
+        break;
+#define KF_GG(P)                                                                            \
+    case 100 + P:                                                                           \
+        if constexpr ((KM & kind_bit(100 + P)) != 0) groupg<S, MODE, P>(t, sb, tb, ps, g, U, src_g, dst_g); \
+        break;
             KF_G1(2) KF_G1(4) KF_G2(4, 2) KF_G2(4, 4)
-            case 3: case 5: case 23: case 25: case 33: case 35: case 43: case 45: case 55:
-                if constexpr (FAM >= FAM_SMOOTH) {
-                    switch (ps.kind) {
-                        KF_G1(3) KF_G1(5)
-                        KF_G2(2, 3) KF_G2(2, 5) KF_G2(3, 3) KF_G2(3, 5) KF_G2(4, 3) KF_G2(4, 5) KF_G2(5, 5)
-                    }
-                }
-                break;
-            case 107: case 111: case 113: case 117: case 119: case 123: case 129: case 131:
-                if constexpr (FAM >= FAM_GENERAL) {
-                    switch (ps.kind) {
-                        KF_GG(7) KF_GG(11) KF_GG(13) KF_GG(17) KF_GG(19) KF_GG(23) KF_GG(29) KF_GG(31)
-                    }
-                }
-                break;
+            KF_G1(3) KF_G1(5)
+            KF_G2(2, 3) KF_G2(2, 5) KF_G2(3, 3) KF_G2(3, 5) KF_G2(4, 3) KF_G2(4, 5) KF_G2(5, 5)
+            KF_GG(7) KF_GG(11) KF_GG(13) KF_GG(17) KF_GG(19) KF_GG(23) KF_GG(29) KF_GG(31)
 #undef KF_G1
 #undef KF_G2
 #undef KF_GG
@@ -365,7 +483,7 @@ KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KPass& ps, bool is_l
 // k == 0: F[0] and F[ncfft]).  When k == ncfft-k the reference writes the
 // bin twice and Fnk is the value that survives.
 template <typename S>
-KF_HD void split_vals(const KSub& sb, int k, cpx<S> Xk, cpx<S> Xnk, cpx<S>& Fk, cpx<S>& Fnk) {
+KF_HD void split_vals(const KTab& tb, int k, cpx<S> Xk, cpx<S> Xnk, cpx<S>& Fk, cpx<S>& Fnk) {
     typedef Ar<S> Arr;
     typedef cpx<S> C;
     if (k == 0) {
@@ -382,7 +500,7 @@ KF_HD void split_vals(const KSub& sb, int k, cpx<S> Xk, cpx<S> Xnk, cpx<S>& Fk, 
     C fpk = Arr::template fixdiv<2>(Xk);
     fpnk = Arr::template fixdiv<2>(fpnk);
     C f1k = c_add(fpk, fpnk), f2k = c_sub(fpk, fpnk);
-    C tw = Arr::cmul(f2k, KF_LDG((const C*)sb.super_tw + (k - 1)));
+    C tw = Arr::cmul(f2k, KF_LDG((const C*)tb.super_tw + (k - 1)));
     Fk.r = Arr::st(Arr::half(Arr::add(f1k.r, tw.r)));
     Fk.i = Arr::st(Arr::half(Arr::add(f1k.i, tw.i)));
     Fnk.r = Arr::st(Arr::half(Arr::sub(f1k.r, tw.r)));
@@ -392,17 +510,19 @@ KF_HD void split_vals(const KSub& sb, int k, cpx<S> Xk, cpx<S> Xnk, cpx<S>& Fk, 
 // The same split reading X from the shared tile (position n lives at
 // input-order index revfull[n]).
 template <typename S>
-KF_HD void r2c_split_pair(const Tile<S>& t, const KSub& sb, int job, int k, cpx<S>& Fk, cpx<S>& Fnk) {
-    cpx<S> Xk = t.sld(KF_LDG(sb.revfull + k), job);
-    cpx<S> Xnk = k == 0 ? Xk : t.sld(KF_LDG(sb.revfull + (sb.L - k)), job);
-    split_vals(sb, k, Xk, Xnk, Fk, Fnk);
+KF_HD void r2c_split_pair(const Tile<S>& t, const KSub& sb, const KTab& tb, int job, int k, cpx<S>& Fk,
+                          cpx<S>& Fnk) {
+    const int* rf = tb.rev + sb.revfull_off;
+    cpx<S> Xk = t.sld(KF_LDG(rf + k), job);
+    cpx<S> Xnk = k == 0 ? Xk : t.sld(KF_LDG(rf + (sb.L - k)), job);
+    split_vals(tb, k, Xk, Xnk, Fk, Fnk);
 }
 
 // Merge of kiss_fftri (kiss_fftr.c:131-153) for work item k: from bins
 // Gk = G[k] and Gnk = G[ncfft-k] (for k == 0: G[0] and G[ncfft]) to the
 // half-size inverse input tmp[k], tmp[ncfft-k].
 template <typename S>
-KF_HD void c2r_merge_pair(const KSub& sb, int k, cpx<S> Gk, cpx<S> Gnk, cpx<S>& tk, cpx<S>& tnk) {
+KF_HD void c2r_merge_pair(const KTab& tb, int k, cpx<S> Gk, cpx<S> Gnk, cpx<S>& tk, cpx<S>& tnk) {
     typedef Ar<S> Arr;
     typedef cpx<S> C;
     if (k == 0) {
@@ -419,7 +539,7 @@ KF_HD void c2r_merge_pair(const KSub& sb, int k, cpx<S> Gk, cpx<S> Gnk, cpx<S>& 
     fk = Arr::template fixdiv<2>(fk);
     fnkc = Arr::template fixdiv<2>(fnkc);
     C fek = c_add(fk, fnkc), d = c_sub(fk, fnkc);
-    C fok = Arr::cmul(d, KF_LDG((const C*)sb.super_tw + (k - 1)));
+    C fok = Arr::cmul(d, KF_LDG((const C*)tb.super_tw + (k - 1)));
     tk = c_add(fek, fok);
     tnk = c_sub(fek, fok);
     tnk.i = Arr::st(Arr::neg(tnk.i));
@@ -437,14 +557,14 @@ KF_HD void item_decode(int J, int logJ, int col, int nk, int it, int& job, int& 
 
 // R2C: split from shared memory straight to the output bins in HBM.
 template <typename S>
-KF_HD void r2c_post(const Tile<S>& t, const KSub& sb, int tid, int T) {
+KF_HD void r2c_post(const Tile<S>& t, const KSub& sb, const KTab& tb, int tid, int T) {
     const int ncfft = sb.L, nk = ncfft / 2 + 1;
     for (int it = tid; it < t.J * nk; it += T) {
         int job, k;
         item_decode(t.J, t.logJ, t.col, nk, it, job, k);
         if (!t.valid(job)) continue;
         cpx<S> Fk, Fnk;
-        r2c_split_pair(t, sb, job, k, Fk, Fnk);
+        r2c_split_pair(t, sb, tb, job, k, Fk, Fnk);
         cpx<S>* o = (cpx<S>*)t.out + t.outb[job];
         if (k != ncfft - k) o[(long long)k * t.out_stride] = Fk;
         o[(long long)(ncfft - k) * t.out_stride] = Fnk;
@@ -453,7 +573,7 @@ KF_HD void r2c_post(const Tile<S>& t, const KSub& sb, int tid, int T) {
 
 // C2R: merge from the input bins in HBM into the shared tile (input order).
 template <typename S>
-KF_HD void c2r_pre(const Tile<S>& t, const KSub& sb, int tid, int T) {
+KF_HD void c2r_pre(const Tile<S>& t, const KSub& sb, const KTab& tb, int tid, int T) {
     const int ncfft = sb.L, nk = ncfft / 2 + 1;
     for (int it = tid; it < t.J * nk; it += T) {
         int job, k;
@@ -463,7 +583,7 @@ KF_HD void c2r_pre(const Tile<S>& t, const KSub& sb, int tid, int T) {
         cpx<S> Gk = f[(long long)k * t.in_stride];
         cpx<S> Gnk = f[(long long)(ncfft - k) * t.in_stride];
         cpx<S> tk, tnk;
-        c2r_merge_pair(sb, k, Gk, Gnk, tk, tnk);
+        c2r_merge_pair(tb, k, Gk, Gnk, tk, tnk);
         if (k == 0) {
             t.sst(0, job, tk);
         } else {
@@ -477,8 +597,8 @@ KF_HD void c2r_pre(const Tile<S>& t, const KSub& sb, int tid, int T) {
 // merge (inverse plan).  Reads every bin pair before any write: the caller
 // places a barrier between fir_mid_compute and fir_mid_store.
 template <typename S>
-KF_HD void fir_mid_compute(const Tile<S>& t, const KSub& fw, const KSub& iv, const cpx<S>* H, int tid, int T,
-                           cpx<S>* outv) {
+KF_HD void fir_mid_compute(const Tile<S>& t, const KSub& fw, const KTab& fwt, const KTab& ivt, const cpx<S>* H,
+                           int tid, int T, cpx<S>* outv) {
     typedef Ar<S> Arr;
     const int ncfft = fw.L, nk = ncfft / 2 + 1;
 #pragma unroll
@@ -489,13 +609,13 @@ KF_HD void fir_mid_compute(const Tile<S>& t, const KSub& fw, const KSub& iv, con
         item_decode(t.J, t.logJ, t.col, nk, it, job, k);
         if (!t.valid(job)) continue;
         cpx<S> Fk, Fnk;
-        r2c_split_pair(t, fw, job, k, Fk, Fnk);
+        r2c_split_pair(t, fw, fwt, job, k, Fk, Fnk);
         int kk = k, knk = ncfft - k;
         if (k == 0) kk = 0, knk = ncfft;
         cpx<S> Gk = Arr::cmul(Fk, KF_LDG(H + kk));
         cpx<S> Gnk = Arr::cmul(Fnk, KF_LDG(H + knk));
         if (k != 0 && k == ncfft - k) Gk = Gnk;
-        c2r_merge_pair(iv, k, Gk, Gnk, outv[2 * i], outv[2 * i + 1]);
+        c2r_merge_pair(ivt, k, Gk, Gnk, outv[2 * i], outv[2 * i + 1]);
     }
 }
 
@@ -522,28 +642,26 @@ KF_HD void fir_mid_store(const Tile<S>& t, const KSub& fw, int tid, int T, const
 // passes: X (or the merged input) sits in HBM in natural order.
 template <typename S>
 KF_HD void split_item(const KArgs& a, long long it) {
-    const KSub& sb = a.sub[0];
-    const int ncfft = sb.L, nk = ncfft / 2 + 1;
+    const int ncfft = a.sub[0].L, nk = ncfft / 2 + 1;
     long long b = it / nk;
     int k = (int)(it - b * nk);
     const cpx<S>* X = (const cpx<S>*)a.in + b * a.in_dhi;
     cpx<S>* F = (cpx<S>*)a.out + b * a.out_dhi;
     cpx<S> Fk, Fnk;
-    split_vals(sb, k, X[k], k == 0 ? X[0] : X[ncfft - k], Fk, Fnk);
+    split_vals(a.tab[0], k, X[k], k == 0 ? X[0] : X[ncfft - k], Fk, Fnk);
     if (k != ncfft - k) F[k] = Fk;
     F[ncfft - k] = Fnk;
 }
 
 template <typename S>
 KF_HD void merge_item(const KArgs& a, long long it) {
-    const KSub& sb = a.sub[0];
-    const int ncfft = sb.L, nk = ncfft / 2 + 1;
+    const int ncfft = a.sub[0].L, nk = ncfft / 2 + 1;
     long long b = it / nk;
     int k = (int)(it - b * nk);
     const cpx<S>* G = (const cpx<S>*)a.in + b * a.in_dhi;
     cpx<S>* X = (cpx<S>*)a.out + b * a.out_dhi;
     cpx<S> tk, tnk;
-    c2r_merge_pair(sb, k, G[k], G[ncfft - k], tk, tnk);
+    c2r_merge_pair(a.tab[0], k, G[k], G[ncfft - k], tk, tnk);
     if (k == 0) {
         X[0] = tk;
     } else {
@@ -553,9 +671,9 @@ KF_HD void merge_item(const KArgs& a, long long it) {
 }
 
 // Job table entries for tile slot j (any thread may fill one).
-KF_HD void job_entry(const KArgs& a, long long tile, int j, long long& inb, long long& outb, int& U, long long& lin,
-                     long long& lout) {
-    long long jg = tile * a.J + j;
+KF_HD void job_entry(const KArgs& a, long long tile, int J, int j, long long& inb, long long& outb, int& U,
+                     long long& lin, long long& lout) {
+    long long jg = tile * J + j;
     if (jg >= a.G) {
         inb = -1;
         outb = -1;

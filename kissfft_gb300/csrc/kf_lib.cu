@@ -450,6 +450,47 @@ const char* kfg_last_error(void) { return g_err.c_str(); }
 
 int kfg_next_fast_size(int n) { return next_fast_size(n); }
 
+int kfg_set_specialize(int on) {
+    set_specialize(on);
+    return KFG_OK;
+}
+
+int kfg_plan_prepare(kfg_plan* p, long long batch, long long in_dist, long long out_dist) {
+    if (!p || batch < 1) return fail(KFG_EINVAL, "kfg_plan_prepare: bad arguments");
+    if (!specialize_enabled()) return KFG_OK;
+    Schedule s;
+    size_t ib = 0, ob = 0;
+    int rc = KFG_OK;
+    if (p->kind == K_FIR) {
+        const long long nx = batch;  // signal length for a FIR plan
+        if (!schedule_fastfir(p->main->p, p->aux->p, p->ntaps, nx, 0, s)) return fail(KFG_EINVAL, s.error);
+    } else {
+        rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
+        if (rc) return rc;
+    }
+    for (auto& st : s.steps) {
+        if (st.kind != 0) continue;
+        std::string err;
+        if (!spec_kernel(st, err)) return fail(KFG_EUNSUPPORTED, err);
+    }
+    return KFG_OK;
+}
+
+int kfg_specialize_check(int dtype, int real, int n, int inverse, long long batch) {
+    Plan p;
+    if (!p.build(dtype, real ? n / 2 : n, inverse, 0, real ? n : 0)) return fail(KFG_EINVAL, p.error);
+    Schedule s;
+    bool ok = real ? (inverse ? schedule_c2r(p, batch, n / 2 + 1, n, s) : schedule_r2c(p, batch, n, n / 2 + 1, s))
+                   : schedule_c2c(p, batch, n, 1, n, s);
+    if (!ok) return fail(KFG_EINVAL, s.error);
+    for (auto& st : s.steps) {
+        if (st.kind != 0) continue;
+        std::string err;
+        if (!spec_compile_only(st, err)) return fail(KFG_EUNSUPPORTED, err);
+    }
+    return KFG_OK;
+}
+
 int kfg_plan_info(const kfg_plan* p, int* out, int nout) {
     if (!p || !out) return KFG_EINVAL;
     int v[6] = {p->kind, p->dtype, (int)p->n, 0, 0, 0};

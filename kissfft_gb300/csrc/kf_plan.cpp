@@ -1,6 +1,7 @@
 // Host-side plans and launch schedules.  Compiled with -ffp-contract=off:
 // the twiddle expressions must round exactly like the reference's.
 #include "kf_plan.h"
+#include "kf_shape.h"
 
 #include <math.h>
 #include <string.h>
@@ -20,22 +21,10 @@ int dtype_size(int dtype) {
 }
 
 std::vector<int> factor(int n) {
-    std::vector<int> f;
-    if (n <= 1) {
-        f.push_back(1);
-        return f;
-    }
-    int p = 4;
-    const double lim = floor(sqrt((double)n));
-    while (n > 1) {
-        while (n % p) {
-            p = (p == 4) ? 2 : (p == 2 ? 3 : p + 2);
-            if (p > lim) p = n;
-        }
-        n /= p;
-        f.push_back(p);
-    }
-    return f;
+    int f[64] = {};
+    int k = factor_into(n, f);
+    if (k > 64) k = 64;
+    return std::vector<int>(f, f + k);
 }
 
 int next_fast_size(int n) {
@@ -97,107 +86,9 @@ void make_super_twiddles(int dtype, int ncfft, int inverse, void* out) {
     }
 }
 
-int max_tile_len(int dtype) {
-    // one tile of at most 128 KiB of shared memory
-    return (128 * 1024) / cpx_size(dtype);
-}
+int max_tile_len(int dtype) { return tile_len_max(dtype); }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-static bool is_small_prime(int p) {
-    return p == 7 || p == 11 || p == 13 || p == 17 || p == 19 || p == 23 || p == 29 || p == 31;
-}
-
-// Build sub-plan over global stages [g0, g1).
-static void build_sub(KSub& sb, int n, int inverse, const std::vector<int>& rad, const std::vector<int>& m,
-                      const std::vector<int>& fs, const std::vector<int>& twoff, int g0, int g1,
-                      std::vector<int>& rev, int pair_rmax) {
-    memset(&sb, 0, sizeof(sb));
-    const int nst = g1 - g0;
-    sb.N = n;
-    sb.nst = nst;
-    sb.inverse = inverse;
-    sb.m_low = m[g1 - 1];
-    long long L = 1;
-    for (int j = g0; j < g1; ++j) L *= rad[j];
-    sb.L = (int)L;
-    for (int i = 0; i < nst; ++i) {
-        int j = g0 + i;
-        KStage& s = sb.st[i];
-        s.p = rad[j];
-        s.m = m[j];
-        s.fs = fs[j];
-        s.tw_off = twoff[j];
-        s.mloc = m[j] / sb.m_low;
-        s.iloc = fs[j] / fs[g0];
-    }
-    // passes, execution order: from the leaf stage down to stage 0
-    std::vector<KPass> ps;
-    int i = nst - 1;
-    while (i >= 0) {
-        KPass p;
-        memset(&p, 0, sizeof(p));
-        int pa = sb.st[i].p;
-        if (i >= 1 && pa >= 2 && pa <= 5 && sb.st[i - 1].p >= 2 && sb.st[i - 1].p <= 5 &&
-            pa * sb.st[i - 1].p <= pair_rmax) {
-            p.a = i - 1;
-            p.ns = 2;
-            p.kind = 10 * sb.st[i - 1].p + pa;
-            p.R = sb.st[i - 1].p * pa;
-            i -= 2;
-        } else {
-            p.a = i;
-            p.ns = 1;
-            // p == 1 only for nfft == 1: the reference's p = 1 generic butterfly
-            p.kind = (pa >= 2 && pa <= 5) ? pa : (is_small_prime(pa) ? 100 + pa : KIND_RT_GENERIC);
-            p.R = pa;
-            i -= 1;
-        }
-        ps.push_back(p);
-    }
-    sb.npass = (int)ps.size();
-    for (int k = 0; k < sb.npass; ++k) {
-        KPass& p = ps[k];
-        const int b = p.a + p.ns - 1;
-        p.H = sb.st[p.a].iloc;
-        p.ML = sb.st[b].mloc;
-        p.rev_off = -1;
-        const bool last = (k == sb.npass - 1);
-        if (p.ML > 1) {
-            p.rev_off = (int)rev.size();
-            rev.resize(rev.size() + p.ML);
-            for (int idx = 0; idx < p.ML; ++idx) {
-                int rem = idx, ul = 0;
-                for (int j = b + 1; j < nst; ++j) {
-                    int d = rem % sb.st[j].p;
-                    rem /= sb.st[j].p;
-                    ul += d * sb.st[j].mloc;
-                }
-                // idx is the input-order index ulp; ul its position
-                if (last)
-                    rev[p.rev_off + ul] = idx;
-                else
-                    rev[p.rev_off + idx] = ul;
-            }
-        }
-        sb.ps[k] = p;
-    }
-}
-
-static int build_revfull(KSub& sb, std::vector<int>& rev) {
-    int off = (int)rev.size();
-    rev.resize(rev.size() + sb.L);
-    for (int A = 0; A < sb.L; ++A) {
-        int rem = A, pos = 0;
-        for (int j = 0; j < sb.nst; ++j) {
-            int d = rem % sb.st[j].p;
-            rem /= sb.st[j].p;
-            pos += d * sb.st[j].mloc;
-        }
-        rev[off + pos] = A;
-    }
-    return off;
-}
 
 bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
     dtype = dtype_;
@@ -205,124 +96,102 @@ bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
     inverse = inverse_ ? 1 : 0;
     real_nfft = real_nfft_;
     error.clear();
-    if (n < 1) {
-        error = "transform length must be positive";
-        return false;
-    }
     if (dtype_size(dtype) == 0) {
         error = "unknown sample type";
         return false;
     }
-    if (lmax <= 0) lmax = max_tile_len(dtype);
-    radix = factor(n);
-    const int K = (int)radix.size();
-    if (K > KF_MAXST) {
-        error = "too many factors";
-        return false;
+    const ShapeInfo si = make_shape(dtype, n, inverse, lmax, real_nfft);
+    switch (si.error) {
+        case 0: break;
+        case 1: error = "transform length must be positive"; return false;
+        case 2: error = "too many factors"; return false;
+        case 3:
+            error = "transform length has no split into two tiles of at most " +
+                    std::to_string(lmax > 0 ? lmax : max_tile_len(dtype));
+            return false;
+        default: error = "generic radix tile too long"; return false;
     }
-    std::vector<int> m(K), fs(K), twoff(K, -1);
-    {
-        long long f = 1;
-        for (int j = 0; j < K; ++j) {
-            fs[j] = (int)f;
-            f *= radix[j];
-            m[j] = (int)(n / f);
-        }
-    }
+    radix.assign(si.radix, si.radix + si.K);
+    nsub = si.nsub;
+    split = si.split;
+    sub[0] = si.sub[0];
+    sub[1] = si.sub[1];
     const int esz = cpx_size(dtype);
     std::vector<uint8_t> twf((size_t)n * esz);
     make_twiddles(dtype, n, inverse, twf.data());
-    // compact per-stage tables: (q, u) -> tw[q*u*fs], plus the radix-3/5 constants
-    std::vector<uint8_t> tws;
-    size_t cnt = 0;
-    for (int j = 0; j < K; ++j) {
-        int p = radix[j];
-        if (p > 5) continue;
-        twoff[j] = (int)cnt;
-        cnt += (size_t)(p - 1) * m[j] + 2;
+    // compact per-stage tables (layout of kf_shape.h: tw_width(p) entries per u)
+    std::vector<uint8_t> tws((size_t)std::max<long long>(si.tw_count, 1) * esz, 0);
+    for (int j = 0; j < si.K; ++j) {
+        const int p = si.radix[j];
+        if (si.twoff[j] < 0) continue;
+        const int W = tw_width(p);
+        uint8_t* base = tws.data() + (size_t)si.twoff[j] * esz;
+        for (int u = 0; u < si.m[j]; ++u)
+            for (int q = 1; q < p; ++q)
+                memcpy(base + ((size_t)u * W + (q - 1)) * esz, twf.data() + (size_t)q * u * si.fs[j] * esz, esz);
+        uint8_t* cst = base + (size_t)W * si.m[j] * esz;
+        memcpy(cst, twf.data() + ((size_t)si.fs[j] * si.m[j] % n) * esz, esz);
+        memcpy(cst + esz, twf.data() + ((size_t)2 * si.fs[j] * si.m[j] % n) * esz, esz);
     }
-    tws.resize(std::max<size_t>(cnt, 1) * esz);
-    for (int j = 0; j < K; ++j) {
-        int p = radix[j];
-        if (p > 5) continue;
-        uint8_t* base = tws.data() + (size_t)twoff[j] * esz;
-        for (int q = 1; q < p; ++q)
-            for (int u = 0; u < m[j]; ++u)
-                memcpy(base + ((size_t)(q - 1) * m[j] + u) * esz, twf.data() + (size_t)q * u * fs[j] * esz, esz);
-        uint8_t* cst = base + (size_t)(p - 1) * m[j] * esz;
-        memcpy(cst, twf.data() + ((size_t)fs[j] * m[j] % n) * esz, esz);
-        memcpy(cst + esz, twf.data() + ((size_t)2 * fs[j] * m[j] % n) * esz, esz);
-    }
-    // split into one or two sub-plans; two-stage register groups hold up
-    // to 25 elements (16 for double, whose elements take 4 registers)
-    const int prm = dtype == KF_F64 ? 16 : 25;
-    std::vector<int> rev;
-    if (n <= lmax) {
-        nsub = 1;
-        split = 0;
-        build_sub(sub[0], n, inverse, radix, m, fs, twoff, 0, K, rev, prm);
-    } else {
-        int best = -1;
-        long long bestv = 0;
-        long long P = 1;
-        for (int s = 1; s < K; ++s) {
-            P *= radix[s - 1];
-            long long LA = n / P;
-            if (P <= lmax && LA <= lmax) {
-                long long v = std::max(P, LA);
-                if (best < 0 || v < bestv) best = s, bestv = v;
-            }
-        }
-        if (best < 0) {
-            error = "transform length has no split into two tiles of at most " + std::to_string(lmax);
-            return false;
-        }
-        nsub = 2;
-        split = best;
-        build_sub(sub[0], n, inverse, radix, m, fs, twoff, best, K, rev, prm);
-        build_sub(sub[1], n, inverse, radix, m, fs, twoff, 0, best, rev, prm);
-    }
+    // digit-reversal tables at the offsets make_shape assigned
+    std::vector<int> rev((size_t)std::max(si.rev_total, 1), 0);
     for (int s = 0; s < nsub; ++s) {
-        for (int k = 0; k < sub[s].npass; ++k)
-            if (sub[s].ps[k].kind == KIND_RT_GENERIC && sub[s].L > KF_MAXO * KF_MAXT) {
-                error = "generic radix tile too long";
-                return false;
+        const KSub& sb = sub[s];
+        for (int k = 0; k < sb.npass; ++k) {
+            const KPass& p = sb.ps[k];
+            if (p.ML <= 1) continue;
+            const int b = p.a + p.ns - 1;
+            const bool last = (k == sb.npass - 1);
+            for (int idx = 0; idx < p.ML; ++idx) {
+                int rem = idx, ul = 0;
+                for (int j = b + 1; j < sb.nst; ++j) {
+                    int d = rem % sb.st[j].p;
+                    rem /= sb.st[j].p;
+                    ul += d * sb.st[j].mloc;
+                }
+                // idx is the input-order index of the lower digits, ul their position
+                if (last)
+                    rev[p.rev_off + ul] = idx;
+                else
+                    rev[p.rev_off + idx] = ul;
             }
-        revfull_off[s] = nsub == 1 ? build_revfull(sub[s], rev) : -1;
+        }
+        if (sb.revfull_off >= 0) {
+            for (int A = 0; A < sb.L; ++A) {
+                int rem = A, pos = 0;
+                for (int j = 0; j < sb.nst; ++j) {
+                    int d = rem % sb.st[j].p;
+                    rem /= sb.st[j].p;
+                    pos += d * sb.st[j].mloc;
+                }
+                rev[sb.revfull_off + pos] = A;
+            }
+        }
     }
     std::vector<uint8_t> sup;
     if (real_nfft > 0) {
         sup.resize((size_t)std::max(1, n / 2) * esz);
         make_super_twiddles(dtype, n, inverse, sup.data());
     }
-    // blob
     off_tw_full = 0;
     off_tw_stage = align256(twf.size());
     off_super = off_tw_stage + align256(tws.size());
     off_rev = off_super + align256(sup.size());
-    blob.assign(off_rev + align256(std::max<size_t>(rev.size(), 1) * sizeof(int)), 0);
+    blob.assign(off_rev + align256(rev.size() * sizeof(int)), 0);
     memcpy(blob.data() + off_tw_full, twf.data(), twf.size());
     memcpy(blob.data() + off_tw_stage, tws.data(), tws.size());
     if (!sup.empty()) memcpy(blob.data() + off_super, sup.data(), sup.size());
-    if (!rev.empty()) memcpy(blob.data() + off_rev, rev.data(), rev.size() * sizeof(int));
-    for (int s = 0; s < nsub; ++s) {
-        sub[s].tw_full = (const void*)(uintptr_t)off_tw_full;
-        sub[s].tw_stage = (const void*)(uintptr_t)off_tw_stage;
-        sub[s].super_tw = real_nfft > 0 ? (const void*)(uintptr_t)off_super : nullptr;
-        sub[s].rev = (const int*)(uintptr_t)off_rev;
-    }
+    memcpy(blob.data() + off_rev, rev.data(), rev.size() * sizeof(int));
+    tab = KTab{};
     return true;
 }
 
 void Plan::bind(const void* base) {
     const uint8_t* b = (const uint8_t*)base;
-    for (int s = 0; s < nsub; ++s) {
-        sub[s].tw_full = b + off_tw_full;
-        sub[s].tw_stage = b + off_tw_stage;
-        sub[s].super_tw = real_nfft > 0 ? (const void*)(b + off_super) : nullptr;
-        sub[s].rev = (const int*)(b + off_rev);
-        sub[s].revfull = revfull_off[s] >= 0 ? (const int*)(b + off_rev) + revfull_off[s] : nullptr;
-    }
+    tab.tw_full = b + off_tw_full;
+    tab.tw_stage = b + off_tw_stage;
+    tab.super_tw = real_nfft > 0 ? (const void*)(b + off_super) : nullptr;
+    tab.rev = (const int*)(b + off_rev);
 }
 
 // ------------------------------------------------------------- launch shapes
@@ -372,24 +241,22 @@ LaunchCfg default_cfg(const KSub& sb, int dtype, int mode, long long G, int col_
 }
 
 // ------------------------------------------------------------- schedules
-static KArgs base_args(const KSub& sb) {
+static void set_shape(Step& st, const Plan& p, int sub) {
+    st.shape_n = p.n;
+    st.shape_inv = p.inverse;
+    st.shape_sub = sub;
+}
+
+static KArgs base_args(const Plan& p, int s) {
     KArgs a;
     memset(&a, 0, sizeof(a));
-    a.sub[0] = sb;
+    a.sub[0] = p.sub[s];
+    a.tab[0] = p.tab;
     a.nsub = 1;
     return a;
 }
 
-int sub_family(const KSub& sb) {
-    int f = FAM_POW2;
-    for (int k = 0; k < sb.npass; ++k) {
-        int kd = sb.ps[k].kind;
-        if (kd == 2 || kd == 4 || kd == 42 || kd == 44) continue;
-        if (kd < 99) f = std::max(f, (int)FAM_SMOOTH);
-        else f = FAM_GENERAL;
-    }
-    return f;
-}
+int sub_family(const KSub& sb) { return family_of(sb); }
 
 static void finish(Step& st, const LaunchCfg& c) {
     st.fam = sub_family(st.args.sub[0]);
@@ -413,7 +280,8 @@ bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long i
         Step st;
         st.mode = MODE_C2C;
         st.dtype = p.dtype;
-        st.args = base_args(p.sub[0]);
+        st.args = base_args(p, 0);
+        set_shape(st, p, 0);
         st.args.G = batch;
         st.args.G_lo = 1;
         st.args.in_dhi = in_dist;
@@ -428,7 +296,8 @@ bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long i
     Step a;
     a.mode = MODE_C2C;
     a.dtype = p.dtype;
-    a.args = base_args(p.sub[0]);
+    a.args = base_args(p, 0);
+    set_shape(a, p, 0);
     a.args.G = batch * Ps;
     a.args.G_lo = Ps;
     a.args.in_dhi = in_dist;
@@ -443,7 +312,8 @@ bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long i
     Step b;
     b.mode = MODE_C2C;
     b.dtype = p.dtype;
-    b.args = base_args(p.sub[1]);
+    b.args = base_args(p, 1);
+    set_shape(b, p, 1);
     b.args.G = batch * LA;
     b.args.G_lo = LA;
     b.args.in_dhi = n;
@@ -468,7 +338,8 @@ static Step elementwise(int kind, const Plan& p, long long batch, long long in_d
     Step st;
     st.kind = kind;
     st.dtype = p.dtype;
-    st.args = base_args(p.sub[0]);
+    st.args = base_args(p, 0);
+    set_shape(st, p, 0);
     st.args.sub[0].L = p.n;  // ncfft for the element kernels
     st.args.G = batch;
     st.args.in_dhi = in_dist;
@@ -496,7 +367,8 @@ bool schedule_r2c(const Plan& p, long long batch, long long in_dist, long long o
         Step st;
         st.mode = MODE_R2C;
         st.dtype = p.dtype;
-        st.args = base_args(p.sub[0]);
+        st.args = base_args(p, 0);
+        set_shape(st, p, 0);
         st.args.G = batch;
         st.args.G_lo = 1;
         st.args.in_dhi = in_dist / 2;
@@ -533,7 +405,8 @@ bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long o
         Step st;
         st.mode = MODE_C2R;
         st.dtype = p.dtype;
-        st.args = base_args(p.sub[0]);
+        st.args = base_args(p, 0);
+        set_shape(st, p, 0);
         st.args.G = batch;
         st.args.G_lo = 1;
         st.args.in_dhi = in_dist;
@@ -572,7 +445,8 @@ bool schedule_axis(const Plan& p, const int* dims, int ndims, int axis, long lon
     Step st;
     st.mode = MODE_C2C;
     st.dtype = p.dtype;
-    st.args = base_args(p.sub[0]);
+    st.args = base_args(p, 0);
+    set_shape(st, p, 0);
     st.in_role = in_role;
     st.out_role = out_role;
     if (S == 1) {
@@ -618,8 +492,10 @@ bool schedule_fastfir(const Plan& fw, const Plan& iv, long long L, long long Ns,
     Step st;
     st.mode = MODE_FIR;
     st.dtype = fw.dtype;
-    st.args = base_args(fw.sub[0]);
+    st.args = base_args(fw, 0);
+    set_shape(st, fw, 0);
     st.args.sub[1] = iv.sub[0];
+    st.args.tab[1] = iv.tab;
     st.args.nsub = 2;
     st.args.G = (nout + ngood - 1) / ngood;
     st.args.G_lo = 1;

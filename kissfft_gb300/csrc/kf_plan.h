@@ -53,13 +53,13 @@ struct Plan {
     // blob = [tw_full | tw_stage | super_tw | rev ints], 256-byte aligned parts
     std::vector<uint8_t> blob;
     size_t off_tw_full = 0, off_tw_stage = 0, off_super = 0, off_rev = 0;
-    int revfull_off[2] = {-1, -1};
-    KSub sub[2];       // pointers hold blob offsets until bound
+    KSub sub[2];       // shapes (kf_shape.h)
+    KTab tab{};        // device tables, set by bind()
     std::string error;
 
     // Builds everything; lmax caps the tile length (0 = dtype default).
     bool build(int dtype, int n, int inverse, int lmax = 0, int real_nfft = 0);
-    // Replace the blob offsets in sub[] with addresses inside base.
+    // Point the tables at a copy of the blob at base.
     void bind(const void* base);
     // Length of each sub-plan's tile.
     int sub_len(int s) const { return sub[s].L; }
@@ -77,6 +77,8 @@ struct Step {
     int kind = 0;       // 0: engine kernel; 1: real split; 2: real merge
     int mode = MODE_C2C;
     int fam = FAM_GENERAL;  // kernel family covering the sub-plans' pass kinds
+    // plan shape of a specialised kernel: make_shape(dtype, shape_n, shape_inv, 0).sub[shape_sub]
+    int shape_n = 0, shape_inv = 0, shape_sub = 0;
     int dtype = KF_F32;
     KArgs args;
     LaunchCfg cfg;

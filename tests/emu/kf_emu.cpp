@@ -17,27 +17,29 @@ using namespace kf;
 
 static int g_force_J = 0, g_force_T = 0;
 
-template <typename S, int MODE, int FAM>
+template <typename S, int MODE, unsigned KM>
 struct CpuExec {
     int T;
     void sync() {}
-    void pass(Tile<S>& t, const KSub& sb, const KPass& ps, bool last, bool sg, bool dg) {
-        for (int tid = 0; tid < T; ++tid) run_pass<S, MODE, FAM>(t, sb, ps, last, tid, T, sg, dg);
+    void pass(Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool last, bool sg, bool dg) {
+        for (int tid = 0; tid < T; ++tid) run_pass<S, MODE, KM>(t, sb, tb, ps, last, tid, T, sg, dg);
     }
-    void rtg(Tile<S>& t, const KSub& sb, const KPass& ps, bool last, bool sg, bool dg) {
+    void rtg(Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool last, bool sg, bool dg) {
         std::vector<cpx<S>> buf((size_t)T * KF_MAXO);
-        for (int tid = 0; tid < T; ++tid) rtg_compute<S, MODE>(t, sb, ps, last, tid, T, sg, &buf[(size_t)tid * KF_MAXO]);
-        for (int tid = 0; tid < T; ++tid) rtg_store<S, MODE>(t, sb, ps, last, tid, T, dg, &buf[(size_t)tid * KF_MAXO]);
+        for (int tid = 0; tid < T; ++tid)
+            rtg_compute<S, MODE>(t, sb, tb, ps, last, tid, T, sg, &buf[(size_t)tid * KF_MAXO]);
+        for (int tid = 0; tid < T; ++tid)
+            rtg_store<S, MODE>(t, sb, tb, ps, last, tid, T, dg, &buf[(size_t)tid * KF_MAXO]);
     }
-    void c2r_pre(Tile<S>& t, const KSub& sb) {
-        for (int tid = 0; tid < T; ++tid) kf::c2r_pre<S>(t, sb, tid, T);
+    void c2r_pre(Tile<S>& t, const KSub& sb, const KTab& tb) {
+        for (int tid = 0; tid < T; ++tid) kf::c2r_pre<S>(t, sb, tb, tid, T);
     }
-    void r2c_post(Tile<S>& t, const KSub& sb) {
-        for (int tid = 0; tid < T; ++tid) kf::r2c_post<S>(t, sb, tid, T);
+    void r2c_post(Tile<S>& t, const KSub& sb, const KTab& tb) {
+        for (int tid = 0; tid < T; ++tid) kf::r2c_post<S>(t, sb, tb, tid, T);
     }
-    void fir_mid(Tile<S>& t, const KSub& fw, const KSub& iv, const cpx<S>* H) {
+    void fir_mid(Tile<S>& t, const KSub& fw, const KTab& fwt, const KTab& ivt, const cpx<S>* H) {
         std::vector<cpx<S>> buf((size_t)T * KF_MAXO);
-        for (int tid = 0; tid < T; ++tid) fir_mid_compute<S>(t, fw, iv, H, tid, T, &buf[(size_t)tid * KF_MAXO]);
+        for (int tid = 0; tid < T; ++tid) fir_mid_compute<S>(t, fw, fwt, ivt, H, tid, T, &buf[(size_t)tid * KF_MAXO]);
         for (int tid = 0; tid < T; ++tid) fir_mid_store<S>(t, fw, tid, T, &buf[(size_t)tid * KF_MAXO]);
     }
 };
@@ -52,7 +54,7 @@ static int run_engine_step_f(const Step& st) {
     int err = 0;
     Tile<S> t;
     memset(&t, 0, sizeof(t));
-    tile_layout(a, t);
+    tile_layout(a, a.sub[0].L, a.J, a.logJ, a.col_in | a.col_out, t);
     t.sm = sm.data();
     t.T = c.T;
     t.inb = inb;
@@ -61,11 +63,11 @@ static int run_engine_step_f(const Step& st) {
     t.lim_in = lin;
     t.lim_out = lout;
     t.err = &err;
-    CpuExec<S, MODE, FAM> x;
+    CpuExec<S, MODE, family_mask(FAM)> x;
     x.T = c.T;
     for (long long tile = 0; tile < a.ntiles; ++tile) {
-        for (int j = 0; j < a.J; ++j) job_entry(a, tile, j, inb[j], outb[j], U[j], lin[j], lout[j]);
-        run_tile<S, MODE, FAM>(x, a, t);
+        for (int j = 0; j < a.J; ++j) job_entry(a, tile, a.J, j, inb[j], outb[j], U[j], lin[j], lout[j]);
+        run_tile<S, MODE, family_mask(FAM)>(x, a, a.sub[0], a.sub[1], t, a.col_in, a.col_out);
     }
     return err;
 }
