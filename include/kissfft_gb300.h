@@ -87,6 +87,10 @@ int kfg_next_fast_size(int n);
  * the shape at run time are used.  Default off; KISSFFT_GB300_SPECIALIZE=1
  * turns it on. */
 int kfg_set_specialize(int on);
+/* TMA staging of contiguous tiles (bulk copy of the next tile's input into
+ * shared memory while the current tile computes).  Default on;
+ * KISSFFT_GB300_TMA=0 turns it off. */
+int kfg_set_tma(int on);
 /* Compile (or load) the specialised kernels a batched call of this shape
  * will use, so that the compile cost is paid here.  For a fast FIR plan,
  * batch is the signal length. */

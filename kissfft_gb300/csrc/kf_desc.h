@@ -97,7 +97,9 @@ struct KArgs {
     int nsub;
     int fir_ngood;
     int use_u;                // 1: twiddle offset U = g_lo (second half of a two-pass plan)
-    int* err;                 // device error word (bounds violations), may be null
+    int tma;                  // 1: tiles are contiguous; stage the next tile by TMA bulk copy
+    int stage_off;            // byte offset of the staging buffer in dynamic shared memory
+    int* err;                 // device error word: bit 0 bad pass kind, bit 1 TMA wait timeout
 };
 
 }  // namespace kf

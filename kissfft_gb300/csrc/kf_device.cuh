@@ -6,8 +6,66 @@
 
 namespace kf {
 
+// ---------------------------------------------------------------- TMA staging
+// One-dimensional bulk copies global -> shared completing on an mbarrier
+// (cp.async.bulk, sm_90+).  Every wait is bounded: past the limit the kernel
+// records bit 1 in the error word and stops using the tile.
+__device__ __forceinline__ unsigned kf_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void kf_mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void kf_fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void kf_fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void kf_bulk_load(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool kf_mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for phase `parity`; false after the limit (about seconds)
+__device__ __forceinline__ bool kf_mbar_wait(unsigned bar, unsigned parity) {
+    for (long long it = 0; it < (1LL << 22); ++it)
+        if (kf_mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 template <typename S, int MODE, unsigned KM>
 struct DevExec {
+    // TMA staging: thread 0 re-arms the staging buffer once the first pass
+    // has read it (next >= 0: the tile to fetch)
+    long long next = -1;
+    unsigned bar = 0, stage = 0;
+    const KArgs* args = nullptr;
+    int L = 0;
+    __device__ void input_consumed() {
+        if (next >= 0 && threadIdx.x == 0) {
+            kf_fence_proxy_async();
+            issue(next);
+        }
+    }
+    __device__ void issue(long long tile) {
+        const long long jg0 = tile * args->J;
+        long long nj = args->G - jg0;
+        if (nj > args->J) nj = args->J;
+        const unsigned bytes = (unsigned)(nj * L * (long long)sizeof(cpx<S>));
+        const cpx<S>* src = (const cpx<S>*)args->in + jg0 * args->in_dhi;
+        kf_bulk_load(stage, src, bytes, bar);
+    }
     __device__ void sync() { __syncthreads(); }
     __device__ void pass(Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool last, bool sg, bool dg) {
         run_pass<S, MODE, KM>(t, sb, tb, ps, last, threadIdx.x, blockDim.x, sg, dg);
@@ -64,8 +122,70 @@ __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, cons
     }
 }
 
+// Tiles of contiguous input (a.tma): persistent CTAs, the next tile's input
+// is bulk-copied into a staging buffer while the current tile runs its
+// passes; the first pass reads the staged tile through shared memory.
+template <typename S, int MODE, unsigned KM, int JF = 0>
+__device__ __forceinline__ void engine_body_tma(const KArgs& a, const KSub& s0) {
+    extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
+    __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
+    __shared__ int s_U[KF_MAXJ];
+    __shared__ __align__(8) unsigned long long s_bar;
+    const int J = JF > 0 ? JF : a.J;
+    const int logJ = JF > 0 ? (JF >= 64 ? 6 : JF >= 32 ? 5 : JF >= 16 ? 4 : JF >= 8 ? 3 : JF >= 4 ? 2 : JF >= 2 ? 1 : 0)
+                            : a.logJ;
+    cpx<S>* stage = (cpx<S>*)(kf_dyn_smem + a.stage_off);
+    Tile<S> t;
+    tile_layout(a, s0.L, J, logJ, 0, t);
+    t.sm = (cpx<S>*)kf_dyn_smem;
+    t.T = blockDim.x;
+    t.inb = s_inb;
+    t.outb = s_outb;
+    t.U = s_U;
+    t.lim_in = s_lin;
+    t.lim_out = s_lout;
+    t.in = stage;  // the first pass reads the staged tile
+    t.in_stride = 1;
+    DevExec<S, MODE, KM> x;
+    x.bar = kf_smem_u32(&s_bar);
+    x.stage = kf_smem_u32(stage);
+    x.args = &a;
+    x.L = s0.L;
+    if (threadIdx.x == 0) {
+        kf_mbar_init(x.bar, 1);
+        kf_fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && (long long)blockIdx.x < a.ntiles) x.issue(blockIdx.x);
+    unsigned parity = 0;
+    for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        for (int j = threadIdx.x; j < J; j += blockDim.x) {
+            job_entry(a, tile, J, j, s_inb[j], s_outb[j], s_U[j], s_lin[j], s_lout[j]);
+            if (s_inb[j] >= 0) s_inb[j] = (long long)j * s0.L;  // offset inside the staging buffer
+        }
+        const bool ok = kf_mbar_wait(x.bar, parity);
+        parity ^= 1u;
+        if (!ok) {
+            if (threadIdx.x == 0 && a.err) atomicOr(a.err, 2);
+            kf_mbar_wait(x.bar, parity ^ 1u);  // give the copy in flight a last chance to land
+            return;
+        }
+        __syncthreads();
+        const long long nxt = tile + gridDim.x;
+        x.next = nxt < a.ntiles ? nxt : -1;
+        run_tile<S, MODE, KM>(x, a, s0, s0, t, 0, 0);
+        __syncthreads();
+    }
+}
+
 template <typename S, int MODE, int FAM>
 __global__ void __launch_bounds__(KF_MAXT) kf_engine_kernel(const __grid_constant__ KArgs a) {
+    if constexpr (MODE == MODE_C2C || MODE == MODE_R2C) {
+        if (a.tma) {
+            engine_body_tma<S, MODE, family_mask(FAM)>(a, a.sub[0]);
+            return;
+        }
+    }
     engine_body<S, MODE, family_mask(FAM)>(a, a.sub[0], a.sub[1]);
 }
 

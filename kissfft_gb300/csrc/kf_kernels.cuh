@@ -10,6 +10,29 @@
 
 namespace kf {
 
+// Grid of a launch: one CTA per tile, or -- for TMA-staged steps, which
+// loop over tiles -- as many CTAs as fit on the GPU at once.
+inline long long launch_grid(const void* k, const Step& st) {
+    long long grid = st.cfg.grid;
+    if (st.args.tma) {
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            if (nsm <= 0) nsm = 1;
+        }
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, st.cfg.T, (size_t)st.cfg.smem) != cudaSuccess ||
+            per <= 0)
+            per = 1;
+        const long long cap = (long long)per * nsm;
+        if (grid > cap) grid = cap;
+    }
+    if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
+    return grid;
+}
+
 template <typename S, int MODE, int FAM>
 static cudaError_t launch_engine_f(const Step& st, cudaStream_t s) {
     auto k = kf_engine_kernel<S, MODE, FAM>;
@@ -19,8 +42,7 @@ static cudaError_t launch_engine_f(const Step& st, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         attr_done = true;
     }
-    long long grid = st.cfg.grid;
-    if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
+    const long long grid = launch_grid((const void*)k, st);
     if (grid <= 0) return cudaSuccess;
     k<<<(unsigned)grid, st.cfg.T, st.cfg.smem, s>>>(st.args);
     return cudaGetLastError();
@@ -57,8 +79,7 @@ const void* spec_kernel(const Step& st, std::string& err);
 bool spec_compile_only(const Step& st, std::string& err);
 
 inline cudaError_t launch_spec(const void* k, const Step& st, cudaStream_t s) {
-    long long grid = st.cfg.grid;
-    if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
+    const long long grid = launch_grid(k, st);
     if (grid <= 0) return cudaSuccess;
     void* args[] = {(void*)&st.args};
     return cudaLaunchKernel(k, dim3((unsigned)grid), dim3(st.cfg.T), args, (size_t)st.cfg.smem, s);

@@ -114,6 +114,7 @@ int run_schedule(Schedule& s, const void* in, void* out, cudaStream_t st, const 
         step.args.in = roles[step.in_role];
         step.args.out = roles[step.out_role];
         step.args.fir_H = firH;
+        enable_tma(step, step.args.in);
         cudaError_t e = launch_step(step, st);
         if (e != cudaSuccess) {
             rc = fail(KFG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -449,6 +450,11 @@ int kfg_synchronize(void) {
 const char* kfg_last_error(void) { return g_err.c_str(); }
 
 int kfg_next_fast_size(int n) { return next_fast_size(n); }
+
+int kfg_set_tma(int on) {
+    set_tma_enabled(on);
+    return KFG_OK;
+}
 
 int kfg_set_specialize(int on) {
     set_specialize(on);

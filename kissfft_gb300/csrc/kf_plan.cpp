@@ -4,6 +4,7 @@
 #include "kf_shape.h"
 
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -257,6 +258,33 @@ static KArgs base_args(const Plan& p, int s) {
 }
 
 int sub_family(const KSub& sb) { return family_of(sb); }
+
+static int g_tma = -1;
+
+void set_tma_enabled(int on) { g_tma = on ? 1 : 0; }
+
+bool tma_enabled() {
+    if (g_tma < 0) {
+        const char* e = getenv("KISSFFT_GB300_TMA");
+        g_tma = (e && e[0] == '0') ? 0 : 1;
+    }
+    return g_tma == 1;
+}
+
+bool enable_tma(Step& st, const void* in) {
+    const KArgs& a = st.args;
+    if (!tma_enabled() || st.kind != 0 || (st.mode != MODE_C2C && st.mode != MODE_R2C)) return false;
+    if (a.col_in || a.col_out || a.in_stride != 1 || a.in_dlo != 0 || a.G_lo != 1) return false;
+    const long long L = a.sub[0].L, esz = cpx_size(st.dtype);
+    if (a.in_dhi != L || (L * esz) % 16 != 0 || ((uintptr_t)in & 15) != 0) return false;
+    const long long stage_off = ((long long)st.cfg.smem + 15) / 16 * 16;
+    const long long total = stage_off + (long long)st.cfg.J * L * esz;
+    if (total > 200 * 1024) return false;
+    st.args.tma = 1;
+    st.args.stage_off = (int)stage_off;
+    st.cfg.smem = (int)total;
+    return true;
+}
 
 static void finish(Step& st, const LaunchCfg& c) {
     st.fam = sub_family(st.args.sub[0]);

@@ -72,6 +72,14 @@ int cfg_min_threads(const KSub& sb, int mode, int J);
 // Smallest kernel family whose compiled pass kinds cover a sub-plan.
 int sub_family(const KSub& sb);
 
+// Stage a step's contiguous tiles by TMA bulk copy when it qualifies: row
+// tiles (C2C/R2C) whose inputs are packed transforms, 16-byte aligned, with
+// room for the staging buffer.  Returns whether staging was switched on.
+struct Step;
+bool enable_tma(Step& st, const void* in);
+void set_tma_enabled(int on);
+bool tma_enabled();
+
 // One kernel launch of a schedule.
 struct Step {
     int kind = 0;       // 0: engine kernel; 1: real split; 2: real merge

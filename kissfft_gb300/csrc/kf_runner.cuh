@@ -25,11 +25,13 @@ KF_HD void run_sub(X& x, Tile<S>& t, const KSub& sb, const KTab& tb, bool src_fi
             if (ps.kind == KIND_RT_GENERIC) {
                 x.rtg(t, sb, tb, ps, last, sg, dg);
                 x.sync();
+                if (first && src_first) x.input_consumed();
                 continue;
             }
         }
         x.pass(t, sb, tb, ps, last, sg, dg);
         x.sync();
+        if (first && src_first) x.input_consumed();
     }
 }
 

@@ -18,6 +18,12 @@ template <typename S, int MODE, int DT, int N, int INV, int LMAX, int SUB, int J
 __global__ void __launch_bounds__(KF_MAXT) kf_spec_kernel(const __grid_constant__ KArgs a) {
     static_assert(kSpecShape<DT, N, INV, LMAX>.error == 0, "plan shape");
     constexpr unsigned KM = kind_mask(kSpecShape<DT, N, INV, LMAX>.sub[SUB]);
+    if constexpr ((MODE == MODE_C2C || MODE == MODE_R2C) && COLIN == 0 && COLOUT == 0) {
+        if (a.tma) {
+            engine_body_tma<S, MODE, KM, J>(a, kSpecShape<DT, N, INV, LMAX>.sub[SUB]);
+            return;
+        }
+    }
     // the fast FIR's second sub-plan is the inverse of the same size
     engine_body<S, MODE, KM, J, COLIN, COLOUT>(a, kSpecShape<DT, N, INV, LMAX>.sub[SUB],
                                                 kSpecShape<DT, N, MODE == MODE_FIR ? 1 : INV, LMAX>.sub[SUB]);

@@ -21,6 +21,7 @@ template <typename S, int MODE, unsigned KM>
 struct CpuExec {
     int T;
     void sync() {}
+    void input_consumed() {}
     void pass(Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool last, bool sg, bool dg) {
         for (int tid = 0; tid < T; ++tid) run_pass<S, MODE, KM>(t, sb, tb, ps, last, tid, T, sg, dg);
     }
