@@ -139,6 +139,8 @@ def run_gpu(args):
     kf.set_specialize(args.specialize)
     t_prep = time.perf_counter()
     for c, (dt, n, b) in zip(cfgs, us):
+        if args.autotune:
+            kf.autotune(c, b)
         kf.prepare(c, b)
     t_prep = time.perf_counter() - t_prep
 
@@ -249,6 +251,8 @@ def main():
                     help="dram bytes per launch of the dominant kernel from an ncu capture")
     ap.add_argument("--specialize", type=int, default=1,
                     help="1: plan-specialised kernels (compiled before warm-up); 0: precompiled family kernels")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: time candidate tile shapes per batch before warm-up (cached on disk)")
     ap.add_argument("--case", action="append", default=[],
                     help="run only these units, TYPE:NFFT:BATCH (profiling runs)")
     args = ap.parse_args()
@@ -304,8 +308,8 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
                 "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
-                "kernels": "plan-specialised (NVRTC, compiled before warm-up in %.1f s)" % r["prepare_s"]
-                if args.specialize else "precompiled families"}
+                "kernels": ("plan-specialised (NVRTC)" if args.specialize else "precompiled families") +
+                ("; autotuned" if args.autotune else "") + "; set-up before warm-up %.1f s" % r["prepare_s"]}
         print(json.dumps(line))
 
 

@@ -155,6 +155,9 @@ int kiss_fft_cuda_status(void);
  * the signal length for a fast FIR cfg). */
 int kiss_fft_cuda_set_specialize(int on);
 int kiss_fft_cuda_prepare(void *cfg, long long batch);
+/* Autotune the launch shapes of batched calls of this size on cfg
+ * (kissfft_gb300.h: kfg_autotune). */
+int kiss_fft_cuda_autotune(void *cfg, long long batch);
 
 #ifdef __cplusplus
 }

@@ -95,6 +95,12 @@ int kfg_set_tma(int on);
  * will use, so that the compile cost is paid here.  For a fast FIR plan,
  * batch is the signal length. */
 int kfg_plan_prepare(kfg_plan *p, long long batch, long long in_dist, long long out_dist);
+/* Autotuner: for each launch of a batched call of this shape, time the
+ * candidate tile shapes (jobs per tile, register budget, TMA staging on or
+ * off) on scratch buffers and keep the fastest for later calls with the
+ * same (batch, in_dist, out_dist).  Results persist in the cache
+ * directory (tune.txt), keyed by plan, shape and GPU. */
+int kfg_autotune(kfg_plan *p, long long batch, long long in_dist, long long out_dist);
 /* Compile, without loading or a GPU, the specialised kernels of a complex
  * (real = 0) or real (real = 1) plan: a check of the embedded sources. */
 int kfg_specialize_check(int dtype, int real, int n, int inverse, long long batch);

@@ -106,6 +106,7 @@ def load(dtype="float"):
         L.kiss_fastfir_cuda_filter.argtypes = [vp, vp, sz, vp]
         L.kiss_fft_cuda_set_stream.argtypes = [vp]
         L.kiss_fft_cuda_prepare.argtypes = [vp, ll]
+        L.kiss_fft_cuda_autotune.argtypes = [vp, ll]
         L.kiss_fft_cuda_last_error.restype = ctypes.c_char_p
         _libs[dtype] = L
     return _libs[dtype]
@@ -344,6 +345,13 @@ def kiss_fastfir_filter(cfg, x, y):
 def set_specialize(on=True):
     """Use kernels compiled (NVRTC, cached on disk) for each plan's exact shape."""
     core().kfg_set_specialize(int(bool(on)))
+
+
+def autotune(cfg, batch):
+    """Time candidate launch shapes for batched calls of this size; keep the fastest."""
+    rc = cfg.lib.kiss_fft_cuda_autotune(ctypes.c_void_p(cfg.ptr), int(batch))
+    if rc:
+        _raise_on_status(cfg.lib, "autotune")
 
 
 def prepare(cfg, batch):

@@ -370,6 +370,18 @@ int kiss_fft_cuda_status(void) { return t_status; }
 
 int kiss_fft_cuda_set_specialize(int on) { return kfg_set_specialize(on); }
 
+int kiss_fft_cuda_autotune(void* cfg, long long batch) {
+    t_status = 0;
+    kiss_fft_cuda_state* s = (kiss_fft_cuda_state*)cfg;
+    if (!s || s->magic != kMagic || !s->plan) {
+        report("kiss_fft_cuda_autotune", "invalid cfg");
+        return KFG_EINVAL;
+    }
+    int rc = note(kfg_autotune(s->plan, batch, 0, 0));
+    if (rc != KFG_OK) report_last("kiss_fft_cuda_autotune");
+    return rc;
+}
+
 int kiss_fft_cuda_prepare(void* cfg, long long batch) {
     t_status = 0;
     kiss_fft_cuda_state* s = (kiss_fft_cuda_state*)cfg;

@@ -338,14 +338,24 @@ KF_HD void group2(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     }
 }
 
-// Generic radix P (a prime 7..31) on registers, kf_bfly_generic
-// (kiss_fft.c:192-233): output leg q1 sums legs q = 0..P-1 in order with
-// twiddle index (q*fstride*k) mod N, k = u + q1*m.
+// Generic radix P (a prime 7..31) on registers.
+//
+// Fixed point follows kf_bfly_generic (kiss_fft.c:192-233) exactly: output
+// leg q1 sums legs q = 0..P-1 in order, each product rounded, with twiddle
+// index (q*fstride*k) mod N, k = u + q1*m.  Since fstride*m = N/P that index
+// is (q*fstride*u + ((q*q1) mod P)*N/P) mod N; for u == 0 (every group of a
+// leaf stage) it takes only the P values r*N/P, so those are loaded once and
+// the fully unrolled sums index them by constants.
+//
+// IEEE types (no bit-exactness to keep, only the error bound) multiply the
+// legs by tw[q*fstride*u] first and then take the size-P DFT on the table's
+// P-th roots, pairing legs q and P-q: about a quarter of the flops.
 template <typename S, int MODE, int P>
 KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, const GroupIx& g, int U,
                   bool src_g, bool dst_g) {
     typedef cpx<S> C;
     typedef Ar<S> Arr;
+    constexpr bool kFixed = sizeof(typename Arr::W) == 4 && (S)0.5 == (S)0;
     const KStage& sa = sb.st[ps.a];
     const C* tw = (const C*)tb.tw_full;
     C x[P];
@@ -359,23 +369,95 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     }
     const int u = g.ul * sb.m_low + U;
     const int N = sb.N;
+    const int NP = sa.fs * sa.m;  // N / P
     GOut<S, MODE> go{};
     if (dst_g) go = gout<S, MODE>(t, g.job, g.pos0);
-#pragma unroll 1
-    for (int q1 = 0; q1 < P; ++q1) {
-        const int step = sa.fs * (u + q1 * sa.m);
-        int twidx = 0;
-        C acc = x[0];
+    C y[P];
+    if constexpr (kFixed) {
+        if (u == 0) {
+            C W[P];
 #pragma unroll
-        for (int q = 1; q < P; ++q) {
-            twidx += step;
-            if (twidx >= N) twidx -= N;
-            acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
+            for (int r = 0; r < P; ++r) W[r] = KF_LDG(tw + r * NP);
+#pragma unroll
+            for (int q1 = 0; q1 < P; ++q1) {
+                C acc = x[0];
+#pragma unroll
+                for (int q = 1; q < P; ++q) acc = c_add(acc, Arr::cmul(x[q], W[(q * q1) % P]));
+                y[q1] = acc;
+            }
+        } else {
+#pragma unroll 1
+            for (int q1 = 0; q1 < P; ++q1) {
+                const int step = sa.fs * (u + q1 * sa.m);
+                int twidx = 0;
+                C acc = x[0];
+#pragma unroll
+                for (int q = 1; q < P; ++q) {
+                    twidx += step;
+                    if (twidx >= N) twidx -= N;
+                    acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
+                }
+                if (dst_g)
+                    go.st(q1 * sa.mloc, acc);
+                else
+                    t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
+            }
+            return;
         }
-        if (dst_g)
-            go.st(q1 * sa.mloc, acc);
-        else
-            t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
+    } else {
+        constexpr int h = (P - 1) / 2;
+        if (u != 0) {
+            int idx = 0;
+            const int step = sa.fs * u;
+#pragma unroll
+            for (int q = 1; q < P; ++q) {
+                idx += step;
+                if (idx >= N) idx -= N;
+                x[q] = Arr::cmul(x[q], KF_LDG(tw + idx));
+            }
+        }
+        C W[h + 1];
+#pragma unroll
+        for (int r = 1; r <= h; ++r) W[r] = KF_LDG(tw + r * NP);
+        C a[h + 1], b[h + 1];
+        C y0 = x[0];
+#pragma unroll
+        for (int q = 1; q <= h; ++q) {
+            a[q].r = x[q].r + x[P - q].r;
+            a[q].i = x[q].i + x[P - q].i;
+            b[q].r = x[q].r - x[P - q].r;
+            b[q].i = x[q].i - x[P - q].i;
+            y0.r += a[q].r;
+            y0.i += a[q].i;
+        }
+        y[0] = y0;
+#pragma unroll
+        for (int q1 = 1; q1 <= h; ++q1) {
+            C A = x[0], B;
+            B.r = 0;
+            B.i = 0;
+#pragma unroll
+            for (int q = 1; q <= h; ++q) {
+                const int k = (q * q1) % P;
+                const S c = k <= h ? W[k].r : W[P - k].r;
+                const S sn = k <= h ? W[k].i : -W[P - k].i;
+                A.r += a[q].r * c;
+                A.i += a[q].i * c;
+                B.r += b[q].r * sn;
+                B.i += b[q].i * sn;
+            }
+            y[q1].r = A.r - B.i;
+            y[q1].i = A.i + B.r;
+            y[P - q1].r = A.r + B.i;
+            y[P - q1].i = A.i - B.r;
+        }
+    }
+    if (dst_g) {
+#pragma unroll
+        for (int q1 = 0; q1 < P; ++q1) go.st(q1 * sa.mloc, y[q1]);
+    } else {
+#pragma unroll
+        for (int q1 = 0; q1 < P; ++q1) t.sst(g.A0 + q1 * sa.iloc, g.job, y[q1]);
     }
 }
 

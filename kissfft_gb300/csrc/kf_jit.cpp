@@ -165,7 +165,7 @@ std::string spec_name(const Step& st) {
     std::ostringstream o;
     o << "kf::kf_spec_kernel<" << scalar_name(st.dtype) << "," << st.mode << "," << st.dtype << "," << st.shape_n
       << "," << st.shape_inv << ",0," << st.shape_sub << "," << st.args.J << "," << st.args.col_in << ","
-      << st.args.col_out << ">";
+      << st.args.col_out << "," << st.cfg.T << "," << st.cfg.minb << ">";
     return o.str();
 }
 
@@ -179,14 +179,18 @@ bool spec_compile_only(const Step& st, std::string& err) {
 // Kernel handle for a step, compiling (or loading from disk) on first use.
 const void* spec_kernel(const Step& st, std::string& err) {
     const std::string name = spec_name(st);
-    std::lock_guard<std::mutex> lk(g_mu);
-    auto it = g_kernels.find(name);
-    if (it != g_kernels.end()) return it->second;
-    auto f = g_failed.find(name);
-    if (f != g_failed.end()) {
-        err = f->second;
-        return nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_kernels.find(name);
+        if (it != g_kernels.end()) return it->second;
+        auto f = g_failed.find(name);
+        if (f != g_failed.end()) {
+            err = f->second;
+            return nullptr;
+        }
     }
+    // compile outside the lock (NVRTC programs compile concurrently); the
+    // first thread to finish registers the kernel
     int ver[2] = {0, 0};
     nvrtcVersion(&ver[0], &ver[1]);
     char key[64];
@@ -197,6 +201,7 @@ const void* spec_kernel(const Step& st, std::string& err) {
     std::string cubin, lowered;
     if (!(read_file(cpath, cubin) && read_file(npath, lowered))) {
         if (!compile(name, cubin, lowered, err)) {
+            std::lock_guard<std::mutex> lk(g_mu);
             g_failed[name] = err;
             return nullptr;
         }
@@ -204,6 +209,9 @@ const void* spec_kernel(const Step& st, std::string& err) {
         write_file(cpath, cubin);
         write_file(npath, lowered);
     }
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_kernels.find(name);
+    if (it != g_kernels.end()) return it->second;
     cudaLibrary_t lib;
     cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e != cudaSuccess) {

@@ -7,9 +7,18 @@
 // plans and host staging is stream-ordered (cudaMallocAsync on the call's
 // stream), never shared between calls.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
 
+#include <algorithm>
+#include <array>
 #include <atomic>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <thread>
 #include <memory>
 #include <string>
 #include <vector>
@@ -96,6 +105,9 @@ struct kfg_plan {
     std::vector<std::unique_ptr<DevPlan>> axes;  // one per axis (nd), or per leading axis (ndr)
     long long ntaps = 0;
     void* d_H = nullptr;
+    // autotuned launch shapes per (batch, in_dist, out_dist): J, minb, tma per step
+    std::mutex tune_mu;
+    std::map<std::string, std::vector<std::array<int, 3>>> tuned;
     ~kfg_plan() {
         if (d_H) cudaFree(d_H);
     }
@@ -248,6 +260,106 @@ int exec_staged(Schedule& s, const void* in, void* out, size_t in_bytes, size_t 
 }
 
 bool valid_dtype(int d) { return d >= KFG_FLOAT && d <= KFG_INT32; }
+
+std::string tune_key(long long batch, long long in_dist, long long out_dist) {
+    std::ostringstream o;
+    o << batch << "/" << in_dist << "/" << out_dist;
+    return o.str();
+}
+
+void apply_cfgs(Schedule& s, const std::vector<std::array<int, 3>>& v) {
+    size_t k = 0;
+    for (auto& st : s.steps) {
+        if (st.kind != 0) continue;
+        if (k >= v.size()) break;
+        const auto& c = v[k++];
+        if (c[0] != st.cfg.J) reshape_step(st, c[0]);
+        st.cfg.minb = c[1];
+        st.tma_ok = c[2];
+    }
+}
+
+void apply_tuned(kfg_plan* p, const std::string& key, Schedule& s) {
+    std::lock_guard<std::mutex> lk(p->tune_mu);
+    auto it = p->tuned.find(key);
+    if (it != p->tuned.end()) apply_cfgs(s, it->second);
+}
+
+// Signature of a plan for the on-disk tuning cache.
+std::string plan_sig(const kfg_plan* p) {
+    std::ostringstream o;
+    o << p->kind << ":" << p->dtype << ":" << p->inverse << ":" << p->n;
+    for (int d : p->dims) o << "x" << d;
+    char name[256] = {0};
+    cudaDeviceProp prop;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess)
+        snprintf(name, sizeof(name), "%s", prop.name);
+    for (char* c = name; *c; ++c)
+        if (*c == ' ') *c = '_';
+    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0);
+    return o.str();
+}
+
+std::string tune_file() {
+    const char* e = getenv("KISSFFT_GB300_CACHE");
+    std::string d;
+    if (e && *e)
+        d = e;
+    else {
+        const char* home = getenv("HOME");
+        d = std::string(home && *home ? home : "/tmp") + "/.cache/kissfft_gb300";
+    }
+    return d + "/tune.txt";
+}
+
+bool tune_load(const std::string& key, std::vector<std::array<int, 3>>& v) {
+    std::ifstream f(tune_file());
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        size_t sp = line.find(' ');
+        if (sp == std::string::npos || line.compare(0, sp, key) != 0 || sp != key.size()) continue;
+        std::istringstream is(line.substr(sp + 1));
+        std::vector<std::array<int, 3>> r;
+        std::array<int, 3> c;
+        while (is >> c[0] >> c[1] >> c[2]) r.push_back(c);
+        v = r;
+        found = true;  // the last line for a key wins
+    }
+    return found;
+}
+
+void tune_store(const std::string& key, const std::vector<std::array<int, 3>>& v) {
+    std::string path = tune_file();
+    std::string dir = path.substr(0, path.rfind('/'));
+    std::string cmd;
+    for (size_t i = 1; i <= dir.size(); ++i)
+        if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
+    std::ofstream f(path, std::ios::app);
+    f << key;
+    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2];
+    f << "\n";
+}
+
+float time_step(Step& st, void* const roles[4], cudaStream_t strm, cudaEvent_t e0, cudaEvent_t e1, int reps) {
+    st.args.in = roles[st.in_role];
+    st.args.out = roles[st.out_role];
+    st.args.tma = 0;
+    enable_tma(st, st.args.in);
+    if (launch_step(st, strm) != cudaSuccess) return -1.f;
+    float best = -1.f;
+    for (int r = 0; r < reps; ++r) {
+        cudaEventRecord(e0, strm);
+        launch_step(st, strm);
+        cudaEventRecord(e1, strm);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best < 0 || ms < best) best = ms;
+    }
+    return best;
+}
 
 }  // namespace
 
@@ -409,6 +521,7 @@ int kfg_exec_batch(kfg_plan* p, const void* in, void* out, long long batch, long
     size_t ib = 0, ob = 0;
     int rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
     if (rc) return rc;
+    apply_tuned(p, tune_key(batch, in_dist, out_dist), s);
     return exec_staged(s, in, out, ib, ob, pick(stream));
 }
 
@@ -473,12 +586,113 @@ int kfg_plan_prepare(kfg_plan* p, long long batch, long long in_dist, long long 
     } else {
         rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
         if (rc) return rc;
+        apply_tuned(p, tune_key(batch, in_dist, out_dist), s);
     }
-    for (auto& st : s.steps) {
-        if (st.kind != 0) continue;
-        std::string err;
-        if (!spec_kernel(st, err)) return fail(KFG_EUNSUPPORTED, err);
+    std::vector<std::string> errs(s.steps.size());
+    std::vector<std::thread> th;
+    for (size_t i = 0; i < s.steps.size(); ++i) {
+        if (s.steps[i].kind != 0) continue;
+        th.emplace_back([&, i]() {
+            if (!spec_kernel(s.steps[i], errs[i]) && errs[i].empty()) errs[i] = "specialised kernel unavailable";
+        });
     }
+    for (auto& t : th) t.join();
+    for (auto& e : errs)
+        if (!e.empty()) return fail(KFG_EUNSUPPORTED, e);
+    return KFG_OK;
+}
+
+int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_dist) {
+    if (!p || batch < 1 || p->kind == K_FIR) return fail(KFG_EINVAL, "kfg_autotune: bad arguments");
+    const std::string key = tune_key(batch, in_dist, out_dist);
+    const std::string dkey = plan_sig(p) + ":" + key;
+    std::vector<std::array<int, 3>> best;
+    if (tune_load(dkey, best)) {
+        std::lock_guard<std::mutex> lk(p->tune_mu);
+        p->tuned[key] = best;
+        return KFG_OK;
+    }
+    Schedule s;
+    size_t ib = 0, ob = 0;
+    int rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
+    if (rc) return rc;
+    void *din = nullptr, *dout = nullptr, *scr = nullptr;
+    const size_t off1 = (s.scratch[0] + 255) & ~(size_t)255;
+    if (cudaMalloc(&din, ib) != cudaSuccess || cudaMalloc(&dout, ob) != cudaSuccess ||
+        (s.scratch[0] + s.scratch[1] > 0 && cudaMalloc(&scr, off1 + s.scratch[1]) != cudaSuccess)) {
+        cudaFree(din);
+        cudaFree(dout);
+        return fail(KFG_ENOMEM, "kfg_autotune: no room for the tuning buffers");
+    }
+    cudaMemset(din, 0, ib);
+    void* roles[4] = {din, dout, scr, (char*)scr + off1};
+    cudaStream_t strm;
+    cudaEvent_t e0, e1;
+    cudaStreamCreate(&strm);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (auto& st0 : s.steps) {
+        if (st0.kind != 0) continue;
+        std::vector<Step> cands;
+        const int J0 = st0.cfg.J;
+        for (int J : {J0 / 2, J0, J0 * 2, J0 * 4}) {
+            Step c = st0;
+            if (J < 1 || (J != J0 && !reshape_step(c, J))) continue;
+            const int m0 = c.cfg.minb;
+            for (int mb : {1, m0, m0 + 1}) {
+                bool dup = false;
+                for (auto& d : cands) dup |= (d.cfg.J == c.cfg.J && d.cfg.minb == mb);
+                if (dup) continue;
+                Step cm = c;
+                cm.cfg.minb = mb;
+                cands.push_back(cm);
+            }
+        }
+        if (specialize_enabled()) {
+            // compile the candidates' kernels in parallel
+            std::vector<std::thread> th;
+            for (auto& c : cands)
+                th.emplace_back([&c]() {
+                    std::string err;
+                    spec_kernel(c, err);
+                });
+            for (auto& t : th) t.join();
+        }
+        float bt = -1.f;
+        std::array<int, 3> bc = {st0.cfg.J, st0.cfg.minb, 1};
+        for (auto& c : cands) {
+            for (int tma = 1; tma >= 0; --tma) {
+                Step x = c;
+                x.tma_ok = tma;
+                float ms = time_step(x, roles, strm, e0, e1, 3);
+                if (ms > 0 && (bt < 0 || ms < bt)) {
+                    bt = ms;
+                    bc = {c.cfg.J, c.cfg.minb, tma};
+                }
+                if (!x.args.tma) break;  // staging not eligible: one timing is enough
+            }
+        }
+        best.push_back(bc);
+        // later steps read what this one wrote: run it once with the winner
+        Step w = st0;
+        std::vector<std::array<int, 3>> one = {bc};
+        Schedule tmp;
+        tmp.steps.push_back(w);
+        apply_cfgs(tmp, one);
+        time_step(tmp.steps[0], roles, strm, e0, e1, 1);
+    }
+    cudaStreamSynchronize(strm);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(strm);
+    cudaFree(din);
+    cudaFree(dout);
+    if (scr) cudaFree(scr);
+    {
+        std::lock_guard<std::mutex> lk(p->tune_mu);
+        p->tuned[key] = best;
+    }
+    tune_store(dkey, best);
     return KFG_OK;
 }
 

@@ -273,7 +273,7 @@ bool tma_enabled() {
 
 bool enable_tma(Step& st, const void* in) {
     const KArgs& a = st.args;
-    if (!tma_enabled() || st.kind != 0 || (st.mode != MODE_C2C && st.mode != MODE_R2C)) return false;
+    if (!tma_enabled() || !st.tma_ok || st.kind != 0 || (st.mode != MODE_C2C && st.mode != MODE_R2C)) return false;
     if (a.col_in || a.col_out || a.in_stride != 1 || a.in_dlo != 0 || a.G_lo != 1) return false;
     const long long L = a.sub[0].L, esz = cpx_size(st.dtype);
     if (a.in_dhi != L || (L * esz) % 16 != 0 || ((uintptr_t)in & 15) != 0) return false;
@@ -286,10 +286,40 @@ bool enable_tma(Step& st, const void* in) {
     return true;
 }
 
+static int default_minb(int T, int smem) {
+    const int by_threads = 2048 / std::max(T, 32);
+    const int by_smem = (227 * 1024) / std::max(smem + 1024, 1);
+    const int by_regs = 65536 / (std::max(T, 32) * 64);  // keep >= 64 registers a thread
+    return std::max(1, std::min(std::min(by_threads, by_smem), std::min(by_regs, 8)));
+}
+
+static void finish(Step& st, const LaunchCfg& c);
+
+bool reshape_step(Step& st, int J) {
+    if (st.kind != 0 || J < 1 || J > KF_MAXJ || (J & (J - 1))) return false;
+    const KSub& sb = st.args.sub[0];
+    LaunchCfg c = st.cfg;
+    int R = 1;
+    for (int k = 0; k < sb.npass; ++k) R = std::max(R, sb.ps[k].R);
+    const long long tpj = std::max(1, sb.L / R);
+    long long T = (tpj * J + 31) / 32 * 32;
+    T = std::max<long long>(T, cfg_min_threads(sb, st.mode, J));
+    if (T > KF_MAXT || cfg_smem_bytes(sb, st.dtype, J) > 200 * 1024) return false;
+    c.J = J;
+    c.T = (int)std::max<long long>(T, 32);
+    c.smem = cfg_smem_bytes(sb, st.dtype, J);
+    c.grid = (st.args.G + J - 1) / J;
+    st.args.tma = 0;
+    st.args.stage_off = 0;
+    finish(st, c);
+    return true;
+}
+
 static void finish(Step& st, const LaunchCfg& c) {
     st.fam = sub_family(st.args.sub[0]);
     if (st.args.nsub > 1) st.fam = std::max(st.fam, sub_family(st.args.sub[1]));
     st.cfg = c;
+    st.cfg.minb = default_minb(c.T, c.smem);
     st.args.J = c.J;
     st.args.col_in = c.col_in;
     st.args.col_out = c.col_out;

@@ -40,6 +40,7 @@ struct LaunchCfg {
     int col_out = 0;  // enumeration of the last pass
     int smem = 0;     // dynamic shared bytes
     long long grid = 0;
+    int minb = 1;     // specialised kernels: blocks per SM the register budget must allow
 };
 
 struct Plan {
@@ -80,11 +81,16 @@ bool enable_tma(Step& st, const void* in);
 void set_tma_enabled(int on);
 bool tma_enabled();
 
+// Re-shape a step: J jobs per tile (T, shared memory and grid follow);
+// false if the shape is not valid for the step.
+bool reshape_step(Step& st, int J);
+
 // One kernel launch of a schedule.
 struct Step {
     int kind = 0;       // 0: engine kernel; 1: real split; 2: real merge
     int mode = MODE_C2C;
     int fam = FAM_GENERAL;  // kernel family covering the sub-plans' pass kinds
+    int tma_ok = 1;         // 0: never stage this step by TMA (autotuner's choice)
     // plan shape of a specialised kernel: make_shape(dtype, shape_n, shape_inv, 0).sub[shape_sub]
     int shape_n = 0, shape_inv = 0, shape_sub = 0;
     int dtype = KF_F32;

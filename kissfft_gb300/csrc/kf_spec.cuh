@@ -13,9 +13,11 @@ namespace kf {
 template <int DT, int N, int INV, int LMAX>
 __device__ constexpr ShapeInfo kSpecShape = make_shape(DT, N, INV, LMAX, 0);
 
-// MODE/J/COLIN/COLOUT fix the launch shape too (J jobs per tile).
-template <typename S, int MODE, int DT, int N, int INV, int LMAX, int SUB, int J, int COLIN, int COLOUT>
-__global__ void __launch_bounds__(KF_MAXT) kf_spec_kernel(const __grid_constant__ KArgs a) {
+// MODE/J/COLIN/COLOUT fix the launch shape too (J jobs per tile); T threads
+// per block and MINB resident blocks per SM bound the registers a thread.
+template <typename S, int MODE, int DT, int N, int INV, int LMAX, int SUB, int J, int COLIN, int COLOUT, int T,
+          int MINB>
+__global__ void __launch_bounds__(T, MINB) kf_spec_kernel(const __grid_constant__ KArgs a) {
     static_assert(kSpecShape<DT, N, INV, LMAX>.error == 0, "plan shape");
     constexpr unsigned KM = kind_mask(kSpecShape<DT, N, INV, LMAX>.sub[SUB]);
     if constexpr ((MODE == MODE_C2C || MODE == MODE_R2C) && COLIN == 0 && COLOUT == 0) {

@@ -1,0 +1,79 @@
+"""The C ABI without a GPU: the built libraries load, export every function
+include/*.h declares, fail loudly (no CPU fallback) when no GPU is present,
+and the run-time specialisation compiles its kernels from the embedded
+sources (NVRTC needs no GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(ROOT, "include")
+
+
+@pytest.fixture(scope="module")
+def libs():
+    from kissfft_gb300 import build
+    if not os.path.exists(build.core_lib()) or any(not os.path.exists(build.dropin_lib(d)) for d in build.DTYPES):
+        build.build()
+    core = ctypes.CDLL(build.core_lib(), mode=ctypes.RTLD_GLOBAL)
+    drop = {d: ctypes.CDLL(build.dropin_lib(d)) for d in build.DTYPES}
+    return core, drop
+
+
+def declared(header):
+    txt = open(os.path.join(INC, header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"\b(k(?:iss|fg)_[a-z0-9_]+)\s*\(", txt)
+    return sorted(set(names))
+
+
+def test_core_exports(libs):
+    core, _ = libs
+    names = declared("kissfft_gb300.h")
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(core, n), n
+
+
+def test_dropin_exports(libs):
+    _, drop = libs
+    names = declared("kiss_fft_cuda.h")
+    assert "kiss_fft_cuda_alloc" in names and "kiss_fftndri_cuda" in names and "kiss_fastfir_cuda" in names
+    for d, L in drop.items():
+        for n in names:
+            assert hasattr(L, n), (d, n)
+
+
+def test_no_cpu_fallback_without_gpu(libs):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    core, drop = libs
+    L = drop["float"]
+    L.kiss_fft_cuda_alloc.restype = ctypes.c_void_p
+    assert not L.kiss_fft_cuda_alloc(1024, 0, None, None)   # NULL like a failed kiss_fft_alloc
+    assert L.kiss_fft_cuda_status() != 0
+
+
+def test_reference_size_rules(libs):
+    core, drop = libs
+    L = drop["float"]
+    L.kiss_fftr_cuda_alloc.restype = ctypes.c_void_p
+    assert not L.kiss_fftr_cuda_alloc(1001, 0, None, None)  # odd real size (kiss_fftr.c:29-32)
+    assert core.kfg_next_fast_size(1001) == 1024
+    assert core.kfg_next_fast_size(7) == 8
+    drop["int16_t"].kiss_fastfir_cuda_alloc.restype = ctypes.c_void_p
+    import numpy as np
+    h = np.ones(16, np.int16)
+    assert not drop["int16_t"].kiss_fastfir_cuda_alloc(h.ctypes.data, 16, None, None, None)
+
+
+@pytest.mark.parametrize("dt,real,n", [(0, 0, 1024), (0, 0, 1000), (2, 0, 3003), (0, 1, 4096), (3, 0, 65536),
+                                       (1, 0, 480), (0, 0, 4099), (2, 1, 6006)])
+def test_specialised_kernels_compile(libs, dt, real, n):
+    core, _ = libs
+    core.kfg_last_error.restype = ctypes.c_char_p
+    rc = core.kfg_specialize_check(dt, real, n, 0, ctypes.c_longlong(4096))
+    assert rc == 0, core.kfg_last_error().decode()

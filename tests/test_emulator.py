@@ -1,0 +1,153 @@
+"""The GPU engine's code run by the CPU emulator, against the oracle (CPU only).
+
+tests/emu/kf_emu.cpp executes the library's launch schedules with the very
+functions the CUDA kernels run (kissfft_gb300/csrc/kf_engine.cuh), one
+thread index at a time.  This checks the plan tables, pass grouping,
+digit-reversal addressing, two-pass splits (forced with small tile limits),
+real split/merge, N-D axis passes and the fast FIR without a GPU.  Fixed
+point must match the oracle bit for bit; float/double within the bound
+2e-7*log2(N) / 1e-15*log2(N) (the IEEE generic-radix butterfly regroups
+its sums).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import inputs
+from oracle import kfo
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EMU = os.path.join(ROOT, "tests", "emu", "_build", "libkfemu.so")
+DT = {"float": 0, "double": 1, "int16_t": 2, "int32_t": 3}
+L = ctypes.c_longlong
+
+
+@pytest.fixture(scope="module")
+def emu():
+    csrc = os.path.join(ROOT, "kissfft_gb300", "csrc")
+    src = os.path.join(ROOT, "tests", "emu", "kf_emu.cpp")
+    deps = [src] + [os.path.join(csrc, f) for f in os.listdir(csrc)]
+    if not os.path.exists(EMU) or os.path.getmtime(EMU) < max(os.path.getmtime(d) for d in deps):
+        os.makedirs(os.path.dirname(EMU), exist_ok=True)
+        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wno-unknown-pragmas", "-shared", "-fPIC",
+                        "-I", csrc, src, os.path.join(csrc, "kf_plan.cpp"), "-o", EMU], check=True)
+    return ctypes.CDLL(EMU)
+
+
+def p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def fixed(dt):
+    return dt in ("int16_t", "int32_t")
+
+
+def check(got, ref_fn, x, dt, n, inv=0):
+    if fixed(dt):
+        assert np.array_equal(got, ref_fn()), (dt, n, inv)
+    else:
+        z = inputs.to_complex128(x, dt)
+        ex = np.fft.ifft(z, axis=-1) * n if inv else np.fft.fft(z, axis=-1)
+        e = np.max(np.linalg.norm(inputs.to_complex128(got, dt) - ex, axis=-1) / np.linalg.norm(ex, axis=-1))
+        bound = (2e-7 if dt == "float" else 1e-15) * max(1.0, np.log2(n))
+        assert e <= bound, (dt, n, inv, e)
+
+
+# (n, lmax): lmax > 0 forces the two-pass split through a small tile
+C2C_CASES = [(1, 0), (2, 0), (3, 0), (7, 0), (8, 0), (12, 0), (30, 0), (97, 0), (120, 0), (480, 0), (1000, 0),
+             (1024, 0), (3003, 0), (4099, 0), (16384, 0), (17017, 0), (65536, 0), (4096, 64), (17017, 256),
+             (65536, 256), (131072, 512), (480, 32), (1000, 40), (961, 31), (8198, 4099)]
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float", "double"])
+def test_c2c(emu, dtype):
+    for n, lmax in C2C_CASES:
+        for inv in (0, 1):
+            x = inputs.cpx((2, n), dtype, n * 7 + inv)
+            y = np.zeros_like(x)
+            rc = emu.emu_c2c(DT[dtype], n, inv, lmax, p(x), p(y), L(2), L(n), L(1), L(n))
+            assert rc == 0, (dtype, n, lmax, rc)
+            check(y, lambda: kfo.fft(x, inv, dtype), x, dtype, n, inv)
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
+def test_stride(emu, dtype):
+    for n, lmax, st in [(480, 0, 3), (1024, 64, 2), (3003, 0, 5)]:
+        x = inputs.cpx((n * st,), dtype, 5)
+        y = kfo.empty_cpx((n,), dtype)
+        assert emu.emu_c2c(DT[dtype], n, 0, lmax, p(x), p(y), L(1), L(n * st), L(st), L(n)) == 0
+        ref = kfo.fft_stride(x, n, st, 0, dtype)
+        if fixed(dtype):
+            assert np.array_equal(y, ref)
+        else:
+            assert np.max(np.abs(y - ref)) <= 1e-3 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float", "double"])
+def test_real(emu, dtype):
+    for nfft, lmax in [(2, 0), (4, 0), (6, 0), (10, 0), (30, 0), (120, 0), (480, 0), (1000, 0), (4096, 0),
+                       (6006, 0), (34034, 0), (34034, 256), (131072, 0)]:
+        t = inputs.real((3, nfft), dtype, nfft)
+        f = kfo.empty_cpx((3, nfft // 2 + 1), dtype)
+        assert emu.emu_r2c(DT[dtype], nfft, lmax, p(t), p(f), L(3)) == 0
+        g = inputs.cpx((3, nfft // 2 + 1), dtype, nfft + 1)
+        t2 = np.zeros((3, nfft), kfo.SCALAR[dtype])
+        assert emu.emu_c2r(DT[dtype], nfft, lmax, p(g), p(t2), L(3)) == 0
+        if fixed(dtype):
+            assert np.array_equal(f, kfo.fftr(t, dtype)), (dtype, nfft, lmax)
+            assert np.array_equal(t2, kfo.fftri(g, nfft, dtype)), (dtype, nfft, lmax)
+        else:
+            ex = np.fft.rfft(t.astype(np.float64), axis=-1)
+            e = np.max(np.linalg.norm(f - ex, axis=-1) / np.linalg.norm(ex, axis=-1))
+            assert e <= (2e-7 if dtype == "float" else 1e-15) * max(1.0, np.log2(nfft)), (dtype, nfft, e)
+            ref2 = kfo.fftri(g, nfft, dtype)
+            e2 = np.max(np.linalg.norm(t2 - ref2, axis=-1) / np.linalg.norm(ref2, axis=-1))
+            assert e2 <= (8e-7 if dtype == "float" else 4e-15) * max(1.0, np.log2(nfft)), (dtype, nfft, e2)
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
+def test_nd_axes(emu, dtype):
+    for dims in [[2, 3], [4, 4], [3, 5, 7], [8, 6], [2, 3, 4, 6], [64, 64], [5, 7, 11]]:
+        for inv in (0, 1):
+            x = inputs.cpx(tuple(dims), dtype, 11)
+            buf = x.copy()
+            d = (ctypes.c_int * len(dims))(*dims)
+            for ax in range(len(dims)):
+                assert emu.emu_axis(DT[dtype], d, len(dims), ax, inv, p(buf)) == 0
+            ref = kfo.fftnd(x, dims, inv, dtype)
+            if fixed(dtype):
+                assert np.array_equal(buf, ref), (dtype, dims, inv)
+            else:
+                assert np.linalg.norm(buf - ref) / np.linalg.norm(ref) < 1e-5
+
+
+def test_fastfir(emu):
+    rng = np.random.default_rng(4)
+    for Lh, Ns in [(255, 20000), (1000, 50000), (17, 5000), (255, 2301), (255, 254)]:
+        h = rng.standard_normal(Lh).astype(np.float32)
+        x = rng.standard_normal(Ns).astype(np.float32)
+        nfft = kfo.fastfir_nfft(Lh)
+        H = np.zeros(nfft // 2 + 1, np.complex64)
+        kfo.lib().kfo_fastfir_response_f32(p(h), L(Lh), L(nfft), p(H))
+        y = np.zeros(max(Ns - Lh + 1, 1), np.float32)
+        assert emu.emu_fastfir(p(H), L(nfft), L(Lh), p(x), L(Ns), p(y)) == 0
+        ref = kfo.fastfir(h, x)
+        # the power-of-two blocks run the exact kf_bfly sequence: same bits
+        assert np.array_equal(y[:ref.size], ref)
+
+
+def test_forced_tile_shapes(emu):
+    """Other jobs-per-tile choices (all tiles partially filled) give the same bits."""
+    for J, T in [(1, 32), (2, 64), (8, 96), (16, 512)]:
+        emu.emu_force(J, T)
+        try:
+            for n in (120, 1000, 3003):
+                x = inputs.cpx((5, n), "int16_t", n)
+                y = np.zeros_like(x)
+                assert emu.emu_c2c(2, n, 0, 0, p(x), p(y), L(5), L(n), L(1), L(n)) == 0
+                assert np.array_equal(y, kfo.fft(x, 0, "int16_t")), (J, T, n)
+        finally:
+            emu.emu_force(0, 0)
