@@ -383,8 +383,12 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
                 C acc = x[0];
 #pragma unroll
                 for (int q = 1; q < P; ++q) acc = c_add(acc, Arr::cmul(x[q], W[(q * q1) % P]));
-                y[q1] = acc;
+                if (dst_g)
+                    go.st(q1 * sa.mloc, acc);
+                else
+                    t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
             }
+            return;
         } else {
 #pragma unroll 1
             for (int q1 = 0; q1 < P; ++q1) {
