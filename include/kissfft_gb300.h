@@ -105,6 +105,34 @@ int kfg_autotune(kfg_plan *p, long long batch, long long in_dist, long long out_
  * (real = 0) or real (real = 1) plan: a check of the embedded sources. */
 int kfg_specialize_check(int dtype, int real, int n, int inverse, long long batch);
 
+/* Device plan cache (the reference's kfc.c: kfc_fft/kfc_ifft keep plans
+ * keyed by size and direction): a shared plan per (real, dtype, n,
+ * inverse), kept until kfg_cache_clear.  Thread-safe. */
+kfg_plan *kfg_plan_cached(int real, int dtype, int n, int inverse);
+int kfg_cache_clear(void);
+
+/* Batched uneven mix: transforms of different sizes, sample types and kinds
+ * in one submission.  Each request reads at in_off and writes at out_off
+ * (bytes, element aligned) of two device arenas given at commit.  Requests
+ * are grouped per plan and run as persistent work-queue launches (one per
+ * sample type, kind and pass), optionally replayed from a CUDA graph. */
+#define KFG_KIND_C2C 1 /* kiss_fft   */
+#define KFG_KIND_R2C 2 /* kiss_fftr  */
+#define KFG_KIND_C2R 3 /* kiss_fftri */
+typedef struct kfg_batch kfg_batch;
+kfg_batch *kfg_batch_create(void);
+int kfg_batch_add(kfg_batch *b, int kind, int dtype, int n, long long in_off, long long out_off);
+/* target_threads: threads per CTA the tiles are widened towards (0 = 256) */
+int kfg_batch_commit(kfg_batch *b, void *in_arena, void *out_arena, int target_threads);
+int kfg_batch_run(kfg_batch *b, void *stream);
+/* capture one run into a CUDA graph; later kfg_batch_run calls replay it */
+int kfg_batch_capture(kfg_batch *b, void *stream);
+/* the plain per-call form of the same work: one drop-in call per request */
+int kfg_batch_run_percall(kfg_batch *b, void *stream);
+/* out[0] requests, out[1] launch steps, out[2] kernel launches, out[3] tiles */
+int kfg_batch_info(const kfg_batch *b, long long *out, int nout);
+void kfg_batch_free(kfg_batch *b);
+
 /* Plan introspection for tests and tools: out[0] = transform kind, out[1] =
  * dtype, out[2] = length, out[3] = number of HBM passes of a 1-D plan,
  * out[4] = kernel family, out[5] = tile length. */

@@ -97,9 +97,26 @@ struct KArgs {
     int nsub;
     int fir_ngood;
     int use_u;                // 1: twiddle offset U = g_lo (second half of a two-pass plan)
+    const long long* in_off;  // per-transform input base (elements), replaces g_hi*in_dhi when set
+    const long long* out_off; // per-transform output base (elements)
     int tma;                  // 1: tiles are contiguous; stage the next tile by TMA bulk copy
     int stage_off;            // byte offset of the staging buffer in dynamic shared memory
     int* err;                 // device error word: bit 0 bad pass kind, bit 1 TMA wait timeout
+};
+
+// A persistent multi-plan launch: CTAs take work items (a step's tile) from
+// an atomic counter; every step carries its own plan shape.
+struct MultiItem {
+    int step;
+    int pad;
+    long long tile;
+};
+
+struct MultiArgs {
+    const KArgs* steps;      // device array of step arguments
+    const MultiItem* items;  // work items, most expensive first
+    long long nitems;
+    unsigned long long* counter;  // zeroed before every launch
 };
 
 }  // namespace kf

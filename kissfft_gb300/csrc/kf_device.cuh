@@ -189,6 +189,41 @@ __global__ void __launch_bounds__(KF_MAXT) kf_engine_kernel(const __grid_constan
     engine_body<S, MODE, family_mask(FAM)>(a, a.sub[0], a.sub[1]);
 }
 
+// Persistent multi-plan kernel: tiles of many plans (one sample type and
+// mode) in one launch, pulled from a work queue.  Every step's shape is read
+// from its KArgs in global memory; blockDim and the shared tile are sized
+// for the largest step of the launch.
+template <typename S, int MODE, unsigned KM>
+__global__ void __launch_bounds__(KF_MAXT) kf_multi_kernel(const __grid_constant__ MultiArgs m) {
+    extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
+    __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
+    __shared__ int s_U[KF_MAXJ];
+    __shared__ unsigned long long s_item;
+    DevExec<S, MODE, KM> x;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(m.counter, 1ull);
+        __syncthreads();
+        const unsigned long long it = s_item;
+        if (it >= (unsigned long long)m.nitems) break;
+        const MultiItem w = m.items[it];
+        const KArgs& a = m.steps[w.step];
+        Tile<S> t;
+        tile_layout(a, a.sub[0].L, a.J, a.logJ, a.col_in | a.col_out, t);
+        t.sm = (cpx<S>*)kf_dyn_smem;
+        t.T = blockDim.x;
+        t.inb = s_inb;
+        t.outb = s_outb;
+        t.U = s_U;
+        t.lim_in = s_lin;
+        t.lim_out = s_lout;
+        for (int j = threadIdx.x; j < a.J; j += blockDim.x)
+            job_entry(a, w.tile, a.J, j, s_inb[j], s_outb[j], s_U[j], s_lin[j], s_lout[j]);
+        __syncthreads();
+        run_tile<S, MODE, KM>(x, a, a.sub[0], a.sub[1], t, a.col_in, a.col_out);
+        __syncthreads();
+    }
+}
+
 template <typename S>
 __global__ void __launch_bounds__(256) kf_split_kernel(const __grid_constant__ KArgs a) {
     const long long items = a.G * (a.sub[0].L / 2 + 1);

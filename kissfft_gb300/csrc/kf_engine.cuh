@@ -768,8 +768,8 @@ KF_HD void job_entry(const KArgs& a, long long tile, int J, int j, long long& in
         return;
     }
     long long ghi = jg / a.G_lo, glo = jg - ghi * a.G_lo;
-    inb = ghi * a.in_dhi + glo * a.in_dlo;
-    outb = ghi * a.out_dhi + glo * a.out_dlo;
+    inb = (a.in_off ? a.in_off[ghi] : ghi * a.in_dhi) + glo * a.in_dlo;
+    outb = (a.out_off ? a.out_off[ghi] : ghi * a.out_dhi) + glo * a.out_dlo;
     U = a.use_u ? (int)glo : 0;
     lin = a.in_limit - inb;
     lout = a.out_limit - outb;

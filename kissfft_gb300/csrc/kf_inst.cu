@@ -37,6 +37,36 @@ cudaError_t KF_NAME(launch_engine_dt, KF_INST_DT, _fam, KF_INST_FAM)(const Step&
     return cudaErrorNotSupported;
 }
 
+cudaError_t KF_NAME(launch_multi_dt, KF_INST_DT, _fam, KF_INST_FAM)(int mode, const MultiArgs& m, int T, int smem,
+                                                                     long long grid, cudaStream_t s) {
+    typedef kf_inst_s S;
+    constexpr unsigned KM = family_mask(KF_INST_FAM);
+    const void* k = nullptr;
+    switch (mode) {
+        case MODE_C2C: k = (const void*)kf_multi_kernel<S, MODE_C2C, KM>; break;
+        case MODE_R2C: k = (const void*)kf_multi_kernel<S, MODE_R2C, KM>; break;
+        case MODE_C2R: k = (const void*)kf_multi_kernel<S, MODE_C2R, KM>; break;
+        default: return cudaErrorNotSupported;
+    }
+    static bool attr_done[3] = {false, false, false};
+    if (!attr_done[mode]) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_done[mode] = true;
+    }
+    if (grid <= 0) {
+        int per = 0, nsm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, T, (size_t)smem) != cudaSuccess || per < 1) per = 1;
+        grid = (long long)per * (nsm > 0 ? nsm : 1);
+        if (grid > m.nitems) grid = m.nitems;
+    }
+    if (grid <= 0) return cudaSuccess;
+    void* args[] = {(void*)&m};
+    return cudaLaunchKernel(k, dim3((unsigned)grid), dim3(T), args, (size_t)smem, s);
+}
+
 #if KF_INST_FAM == 0
 cudaError_t KF_NAME(launch_elem_dt, KF_INST_DT, , )(const Step& st, cudaStream_t s) {
     return launch_elem<kf_inst_s>(st, s);

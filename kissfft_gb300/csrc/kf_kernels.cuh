@@ -71,6 +71,33 @@ KF_DECL_DT(1)
 KF_DECL_DT(2)
 KF_DECL_DT(3)
 #undef KF_DECL_DT
+#define KF_DECL_MULTI(D)                                                                                   \
+    cudaError_t launch_multi_dt##D##_fam0(int, const MultiArgs&, int, int, long long, cudaStream_t);       \
+    cudaError_t launch_multi_dt##D##_fam1(int, const MultiArgs&, int, int, long long, cudaStream_t);       \
+    cudaError_t launch_multi_dt##D##_fam2(int, const MultiArgs&, int, int, long long, cudaStream_t);
+KF_DECL_MULTI(0)
+KF_DECL_MULTI(1)
+KF_DECL_MULTI(2)
+KF_DECL_MULTI(3)
+#undef KF_DECL_MULTI
+
+// grid <= 0: as many CTAs as fit at once
+inline cudaError_t launch_multi(int dtype, int fam, int mode, const MultiArgs& m, int T, int smem, long long grid,
+                                cudaStream_t s) {
+#define KF_CASE_MULTI(D)                                                                   \
+    case D:                                                                               \
+        if (fam == FAM_POW2) return launch_multi_dt##D##_fam0(mode, m, T, smem, grid, s);   \
+        if (fam == FAM_SMOOTH) return launch_multi_dt##D##_fam1(mode, m, T, smem, grid, s); \
+        return launch_multi_dt##D##_fam2(mode, m, T, smem, grid, s);
+    switch (dtype) {
+        KF_CASE_MULTI(0)
+        KF_CASE_MULTI(1)
+        KF_CASE_MULTI(2)
+        KF_CASE_MULTI(3)
+    }
+#undef KF_CASE_MULTI
+    return cudaErrorInvalidValue;
+}
 
 // Run-time specialised kernels (kf_jit.cpp).
 bool specialize_enabled();

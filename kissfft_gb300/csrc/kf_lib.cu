@@ -11,6 +11,8 @@
 #include <string.h>
 #include <sys/stat.h>
 
+#include <math.h>
+
 #include <algorithm>
 #include <array>
 #include <atomic>
@@ -721,6 +723,313 @@ int kfg_plan_info(const kfg_plan* p, int* out, int nout) {
         v[5] = d->p.sub[0].L;
     }
     for (int i = 0; i < nout && i < 6; ++i) out[i] = v[i];
+    return KFG_OK;
+}
+
+}  // extern "C"
+
+// ====================================================================
+// Device plan cache (the GPU counterpart of the reference's kfc.c:24-83:
+// find_cached_fft keyed by (nfft, inverse)); here keyed by transform kind,
+// sample type, size and direction, thread-safe, plans kept until
+// kfg_cache_clear().
+// ====================================================================
+namespace {
+std::mutex g_cache_mu;
+std::map<std::string, kfg_plan*> g_cache;
+}  // namespace
+
+extern "C" kfg_plan* kfg_plan_cached(int real, int dtype, int n, int inverse) {
+    std::ostringstream k;
+    k << real << ":" << dtype << ":" << n << ":" << (inverse ? 1 : 0);
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_cache.find(k.str());
+    if (it != g_cache.end()) return it->second;
+    kfg_plan* p = real ? kfg_plan_real(dtype, n, inverse) : kfg_plan_c2c(dtype, n, inverse);
+    if (p) g_cache[k.str()] = p;
+    return p;
+}
+
+extern "C" int kfg_cache_clear(void) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    for (auto& kv : g_cache) kfg_plan_free(kv.second);
+    g_cache.clear();
+    return KFG_OK;
+}
+
+// ====================================================================
+// Batched uneven mix: many transforms of different sizes, sample types and
+// kinds, their data at byte offsets in two device arenas.  Requests are
+// grouped per plan; the tiles of all groups run in persistent multi-plan
+// launches (one per sample type, mode and pass), CTAs pulling work items
+// from an atomic counter, largest tiles first.  The whole run can be
+// captured in a CUDA graph.
+// ====================================================================
+struct kfg_batch {
+    struct Req {
+        int kind, dtype, n;
+        long long in_off, out_off;
+    };
+    struct Launch {
+        int phase = 0, dtype = 0, mode = 0, fam = 0, T = 32, smem = 0;
+        int elem_step = -1;  // >= 0: a split/merge element step launched on its own
+        std::vector<MultiItem> items;
+        MultiItem* d_items = nullptr;
+        unsigned long long* d_counter = nullptr;
+    };
+    std::vector<Req> reqs;
+    void* in_arena = nullptr;
+    void* out_arena = nullptr;
+    int target_T = 256;
+    bool committed = false;
+    std::vector<Step> steps;
+    KArgs* d_steps = nullptr;
+    std::vector<Launch> launches;
+    std::vector<void*> allocs;
+    std::vector<kfg_plan*> req_plan;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+
+    void release() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+        for (void* p : allocs) cudaFree(p);
+        allocs.clear();
+        launches.clear();
+        steps.clear();
+        d_steps = nullptr;
+        committed = false;
+    }
+    ~kfg_batch() { release(); }
+};
+
+namespace {
+
+template <typename T>
+T* upload(kfg_batch* b, const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    void* d = nullptr;
+    if (cudaMalloc(&d, v.size() * sizeof(T)) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    b->allocs.push_back(d);
+    return (T*)d;
+}
+
+int batch_commit(kfg_batch* b) {
+    b->release();
+    // group requests per plan
+    std::map<std::string, std::vector<int>> groups;
+    b->req_plan.assign(b->reqs.size(), nullptr);
+    for (size_t i = 0; i < b->reqs.size(); ++i) {
+        const auto& r = b->reqs[i];
+        std::ostringstream k;
+        k << r.kind << ":" << r.dtype << ":" << r.n;
+        groups[k.str()].push_back((int)i);
+        const bool real = r.kind != KFG_KIND_C2C;
+        kfg_plan* p = kfg_plan_cached(real, r.dtype, r.n, r.kind == KFG_KIND_C2R);
+        if (!p) return KFG_EINVAL;
+        b->req_plan[i] = p;
+    }
+    std::vector<int> phase_of;
+    for (auto& kv : groups) {
+        const auto& idx = kv.second;
+        kfg_plan* p = b->req_plan[idx[0]];
+        const long long cnt = (long long)idx.size();
+        Schedule s;
+        size_t ib = 0, ob = 0;
+        int rc = build_schedule(p, cnt, 0, 1, 0, s, ib, ob);
+        if (rc) return rc;
+        const int esz = cpx_size(p->dtype);
+        std::vector<long long> io(cnt), oo(cnt);
+        for (long long j = 0; j < cnt; ++j) {
+            const auto& r = b->reqs[idx[j]];
+            if (r.in_off % esz || r.out_off % esz) return fail(KFG_EINVAL, "kfg_batch: offsets must be element aligned");
+            io[j] = r.in_off / esz;
+            oo[j] = r.out_off / esz;
+        }
+        long long* d_io = upload(b, io);
+        long long* d_oo = upload(b, oo);
+        void* scr = nullptr;
+        const size_t off1 = (s.scratch[0] + 255) & ~(size_t)255;
+        if (s.scratch[0] + s.scratch[1] > 0) {
+            if (cudaMalloc(&scr, off1 + s.scratch[1]) != cudaSuccess) return fail(KFG_ENOMEM, "kfg_batch: scratch");
+            b->allocs.push_back(scr);
+        }
+        void* roles[4] = {b->in_arena, b->out_arena, scr, (char*)scr + off1};
+        int ph = 0;
+        for (auto& st : s.steps) {
+            if (st.in_role == 0) st.args.in_off = d_io;
+            if (st.out_role == 1) st.args.out_off = d_oo;
+            if (st.in_role == 0 && st.kind != 0) return fail(KFG_EUNSUPPORTED, "kfg_batch: two-pass real inverse");
+            st.args.in = roles[st.in_role];
+            st.args.out = roles[st.out_role];
+            if (st.kind == 0) {
+                // widen the tile towards the launch's thread target
+                while (st.cfg.T * 2 <= b->target_T) {
+                    Step w = st;
+                    if (!reshape_step(w, st.cfg.J * 2) || w.cfg.T > b->target_T || w.args.ntiles < 1) break;
+                    st = w;
+                }
+            }
+            b->steps.push_back(st);
+            phase_of.push_back(ph++);
+        }
+    }
+    // launches: (phase, dtype, mode, family, tile class); element steps alone
+    std::map<std::string, int> lkey;
+    for (size_t i = 0; i < b->steps.size(); ++i) {
+        const Step& st = b->steps[i];
+        if (st.kind != 0) {
+            kfg_batch::Launch L;
+            L.phase = phase_of[i];
+            L.elem_step = (int)i;
+            b->launches.push_back(L);
+            continue;
+        }
+        std::ostringstream k;
+        k << phase_of[i] << ":" << st.dtype << ":" << st.mode << ":" << st.fam << ":" << (st.cfg.smem > 64 * 1024);
+        auto it = lkey.find(k.str());
+        int li;
+        if (it == lkey.end()) {
+            li = (int)b->launches.size();
+            lkey[k.str()] = li;
+            kfg_batch::Launch L;
+            L.phase = phase_of[i];
+            L.dtype = st.dtype;
+            L.mode = st.mode;
+            L.fam = st.fam;
+            b->launches.push_back(L);
+        } else {
+            li = it->second;
+        }
+        auto& L = b->launches[li];
+        L.T = std::max(L.T, st.cfg.T);
+        L.smem = std::max(L.smem, st.cfg.smem);
+        for (long long t = 0; t < st.args.ntiles; ++t) L.items.push_back(MultiItem{(int)i, 0, t});
+    }
+    // most expensive tiles first (cost ~ J * L * log L)
+    std::vector<double> cost(b->steps.size());
+    for (size_t i = 0; i < b->steps.size(); ++i) {
+        const Step& st = b->steps[i];
+        const double L = st.args.sub[0].L;
+        cost[i] = st.cfg.J * L * (L > 1 ? std::log2(L) : 1.0);
+    }
+    for (auto& L : b->launches) {
+        std::stable_sort(L.items.begin(), L.items.end(),
+                         [&](const MultiItem& a, const MultiItem& c) { return cost[a.step] > cost[c.step]; });
+        L.d_items = upload(b, L.items);
+        void* c = nullptr;
+        if (cudaMalloc(&c, sizeof(unsigned long long)) != cudaSuccess) return fail(KFG_ENOMEM, "kfg_batch: counter");
+        b->allocs.push_back(c);
+        L.d_counter = (unsigned long long*)c;
+    }
+    std::stable_sort(b->launches.begin(), b->launches.end(),
+                     [](const kfg_batch::Launch& a, const kfg_batch::Launch& c) { return a.phase < c.phase; });
+    std::vector<KArgs> ka;
+    for (auto& st : b->steps) ka.push_back(st.args);
+    b->d_steps = upload(b, ka);
+    b->committed = true;
+    return KFG_OK;
+}
+
+int batch_enqueue(kfg_batch* b, cudaStream_t strm) {
+    for (auto& L : b->launches) {
+        cudaError_t e;
+        if (L.elem_step >= 0) {
+            e = launch_step(b->steps[L.elem_step], strm);
+        } else {
+            cudaMemsetAsync(L.d_counter, 0, sizeof(unsigned long long), strm);
+            MultiArgs m;
+            m.steps = b->d_steps;
+            m.items = L.d_items;
+            m.nitems = (long long)L.items.size();
+            m.counter = L.d_counter;
+            e = launch_multi(L.dtype, L.fam, L.mode, m, L.T, L.smem, 0, strm);
+        }
+        if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("kfg_batch launch: ") + cudaGetErrorString(e));
+    }
+    return KFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+kfg_batch* kfg_batch_create(void) { return new kfg_batch; }
+
+void kfg_batch_free(kfg_batch* b) { delete b; }
+
+int kfg_batch_add(kfg_batch* b, int kind, int dtype, int n, long long in_off, long long out_off) {
+    if (!b || !valid_dtype(dtype) || n < 1 || kind < KFG_KIND_C2C || kind > KFG_KIND_C2R || in_off < 0 || out_off < 0)
+        return fail(KFG_EINVAL, "kfg_batch_add: bad arguments");
+    if (kind != KFG_KIND_C2C && (n & 1)) return fail(KFG_EINVAL, "Real FFT optimization must be even.");
+    b->reqs.push_back(kfg_batch::Req{kind, dtype, n, in_off, out_off});
+    b->committed = false;
+    return KFG_OK;
+}
+
+int kfg_batch_commit(kfg_batch* b, void* in_arena, void* out_arena, int target_threads) {
+    if (!b || !in_arena || !out_arena) return fail(KFG_EINVAL, "kfg_batch_commit: bad arguments");
+    b->in_arena = in_arena;
+    b->out_arena = out_arena;
+    if (target_threads > 0) b->target_T = std::min(std::max(target_threads, 32), KF_MAXT);
+    return batch_commit(b);
+}
+
+int kfg_batch_run(kfg_batch* b, void* stream) {
+    if (!b || !b->committed) return fail(KFG_EINVAL, "kfg_batch_run: commit first");
+    cudaStream_t s = pick(stream);
+    if (b->gexec) {
+        KFG_CK(cudaGraphLaunch(b->gexec, s));
+        return KFG_OK;
+    }
+    return batch_enqueue(b, s);
+}
+
+int kfg_batch_capture(kfg_batch* b, void* stream) {
+    if (!b || !b->committed) return fail(KFG_EINVAL, "kfg_batch_capture: commit first");
+    cudaStream_t s = stream ? (cudaStream_t)stream : nullptr;
+    bool own = false;
+    if (!s) {
+        KFG_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        own = true;
+    }
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->gexec = nullptr;
+    b->graph = nullptr;
+    KFG_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = batch_enqueue(b, s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (own) cudaStreamDestroy(s);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    b->graph = g;
+    KFG_CK(cudaGraphInstantiate(&b->gexec, g, 0));
+    return KFG_OK;
+}
+
+int kfg_batch_run_percall(kfg_batch* b, void* stream) {
+    if (!b || !b->in_arena) return fail(KFG_EINVAL, "kfg_batch_run_percall: commit first");
+    if (b->req_plan.size() != b->reqs.size()) return fail(KFG_EINVAL, "kfg_batch_run_percall: commit first");
+    for (size_t i = 0; i < b->reqs.size(); ++i) {
+        const auto& r = b->reqs[i];
+        int rc = kfg_exec_batch(b->req_plan[i], (const char*)b->in_arena + r.in_off, (char*)b->out_arena + r.out_off, 1,
+                                0, 0, stream);
+        if (rc) return rc;
+    }
+    return KFG_OK;
+}
+
+int kfg_batch_info(const kfg_batch* b, long long* out, int nout) {
+    if (!b || !out) return KFG_EINVAL;
+    long long items = 0;
+    for (auto& L : b->launches) items += (long long)L.items.size();
+    long long v[4] = {(long long)b->reqs.size(), (long long)b->steps.size(), (long long)b->launches.size(), items};
+    for (int i = 0; i < nout && i < 4; ++i) out[i] = v[i];
     return KFG_OK;
 }
 

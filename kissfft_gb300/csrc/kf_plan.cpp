@@ -274,7 +274,7 @@ bool tma_enabled() {
 bool enable_tma(Step& st, const void* in) {
     const KArgs& a = st.args;
     if (!tma_enabled() || !st.tma_ok || st.kind != 0 || (st.mode != MODE_C2C && st.mode != MODE_R2C)) return false;
-    if (a.col_in || a.col_out || a.in_stride != 1 || a.in_dlo != 0 || a.G_lo != 1) return false;
+    if (a.col_in || a.col_out || a.in_stride != 1 || a.in_dlo != 0 || a.G_lo != 1 || a.in_off) return false;
     const long long L = a.sub[0].L, esz = cpx_size(st.dtype);
     if (a.in_dhi != L || (L * esz) % 16 != 0 || ((uintptr_t)in & 15) != 0) return false;
     const long long stage_off = ((long long)st.cfg.smem + 15) / 16 * 16;
