@@ -345,7 +345,9 @@ KF_HD void group2(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
 // index (q*fstride*k) mod N, k = u + q1*m.  Since fstride*m = N/P that index
 // is (q*fstride*u + ((q*q1) mod P)*N/P) mod N; for u == 0 (every group of a
 // leaf stage) it takes only the P values r*N/P, so those are loaded once and
-// the fully unrolled sums index them by constants.
+// the fully unrolled sums index them by constants.  That unrolled form is
+// kept to P <= 13: its code grows as P^2, and P = 17..31 (rare leaf radices)
+// would multiply the compile time of every kernel that can meet them.
 //
 // IEEE types (no bit-exactness to keep, only the error bound) multiply the
 // legs by tw[q*fstride*u] first and then take the size-P DFT on the table's
@@ -374,40 +376,41 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     if (dst_g) go = gout<S, MODE>(t, g.job, g.pos0);
     C y[P];
     if constexpr (kFixed) {
-        if (u == 0) {
-            C W[P];
+        if constexpr (P <= 13) {
+            if (u == 0) {
+                C W[P];
 #pragma unroll
-            for (int r = 0; r < P; ++r) W[r] = KF_LDG(tw + r * NP);
+                for (int r = 0; r < P; ++r) W[r] = KF_LDG(tw + r * NP);
 #pragma unroll
-            for (int q1 = 0; q1 < P; ++q1) {
-                C acc = x[0];
+                for (int q1 = 0; q1 < P; ++q1) {
+                    C acc = x[0];
 #pragma unroll
-                for (int q = 1; q < P; ++q) acc = c_add(acc, Arr::cmul(x[q], W[(q * q1) % P]));
-                if (dst_g)
-                    go.st(q1 * sa.mloc, acc);
-                else
-                    t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
-            }
-            return;
-        } else {
-#pragma unroll 1
-            for (int q1 = 0; q1 < P; ++q1) {
-                const int step = sa.fs * (u + q1 * sa.m);
-                int twidx = 0;
-                C acc = x[0];
-#pragma unroll
-                for (int q = 1; q < P; ++q) {
-                    twidx += step;
-                    if (twidx >= N) twidx -= N;
-                    acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
+                    for (int q = 1; q < P; ++q) acc = c_add(acc, Arr::cmul(x[q], W[(q * q1) % P]));
+                    if (dst_g)
+                        go.st(q1 * sa.mloc, acc);
+                    else
+                        t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
                 }
-                if (dst_g)
-                    go.st(q1 * sa.mloc, acc);
-                else
-                    t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
+                return;
             }
-            return;
         }
+#pragma unroll 1
+        for (int q1 = 0; q1 < P; ++q1) {
+            const int step = sa.fs * (u + q1 * sa.m);
+            int twidx = 0;
+            C acc = x[0];
+#pragma unroll
+            for (int q = 1; q < P; ++q) {
+                twidx += step;
+                if (twidx >= N) twidx -= N;
+                acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
+            }
+            if (dst_g)
+                go.st(q1 * sa.mloc, acc);
+            else
+                t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
+        }
+        return;
     } else {
         constexpr int h = (P - 1) / 2;
         if (u != 0) {
@@ -725,14 +728,16 @@ KF_HD void fir_mid_store(const Tile<S>& t, const KSub& fw, int tid, int T, const
 }
 
 // Standalone split / merge items for real plans that run as two HBM
-// passes: X (or the merged input) sits in HBM in natural order.
+// passes: X (or the merged input) sits in HBM in natural order.  Item it
+// belongs to transform it / (ncfft/2+1), found at its in_off / out_off entry
+// when the launch carries per-transform offsets (batched requests).
 template <typename S>
 KF_HD void split_item(const KArgs& a, long long it) {
     const int ncfft = a.sub[0].L, nk = ncfft / 2 + 1;
     long long b = it / nk;
     int k = (int)(it - b * nk);
-    const cpx<S>* X = (const cpx<S>*)a.in + b * a.in_dhi;
-    cpx<S>* F = (cpx<S>*)a.out + b * a.out_dhi;
+    const cpx<S>* X = (const cpx<S>*)a.in + (a.in_off ? a.in_off[b] : b * a.in_dhi);
+    cpx<S>* F = (cpx<S>*)a.out + (a.out_off ? a.out_off[b] : b * a.out_dhi);
     cpx<S> Fk, Fnk;
     split_vals(a.tab[0], k, X[k], k == 0 ? X[0] : X[ncfft - k], Fk, Fnk);
     if (k != ncfft - k) F[k] = Fk;
@@ -744,8 +749,8 @@ KF_HD void merge_item(const KArgs& a, long long it) {
     const int ncfft = a.sub[0].L, nk = ncfft / 2 + 1;
     long long b = it / nk;
     int k = (int)(it - b * nk);
-    const cpx<S>* G = (const cpx<S>*)a.in + b * a.in_dhi;
-    cpx<S>* X = (cpx<S>*)a.out + b * a.out_dhi;
+    const cpx<S>* G = (const cpx<S>*)a.in + (a.in_off ? a.in_off[b] : b * a.in_dhi);
+    cpx<S>* X = (cpx<S>*)a.out + (a.out_off ? a.out_off[b] : b * a.out_dhi);
     cpx<S> tk, tnk;
     c2r_merge_pair(a.tab[0], k, G[k], G[ncfft - k], tk, tnk);
     if (k == 0) {

@@ -862,7 +862,6 @@ int batch_commit(kfg_batch* b) {
         for (auto& st : s.steps) {
             if (st.in_role == 0) st.args.in_off = d_io;
             if (st.out_role == 1) st.args.out_off = d_oo;
-            if (st.in_role == 0 && st.kind != 0) return fail(KFG_EUNSUPPORTED, "kfg_batch: two-pass real inverse");
             st.args.in = roles[st.in_role];
             st.args.out = roles[st.out_role];
             if (st.kind == 0) {
