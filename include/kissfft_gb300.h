@@ -3,8 +3,8 @@
  * run-time tag.
  *
  * This is the layer under the per-type drop-in libraries (kiss_fft_cuda.h):
- * it exposes batched execution, explicit streams and the fast FIR.  Every
- * function here has a counterpart in the reference (mborgerding/kissfft):
+ * it exposes batched execution, explicit streams and the fast FIR.  The
+ * transform calls map onto the reference (mborgerding/kissfft) like this:
  *
  *   kfg_plan_c2c   kiss_fft_alloc      (kiss_fft.h:117,   kiss_fft.c:337-372)
  *   kfg_plan_real  kiss_fftr_alloc     (kiss_fftr.h:29,   kiss_fftr.c:21-61)
@@ -70,6 +70,20 @@ int kfg_exec_stride(kfg_plan *p, const void *in, void *out, int in_stride, void 
  * batch (complex elements or real samples, as the side holds); 0 = packed. */
 int kfg_exec_batch(kfg_plan *p, const void *in, void *out, long long batch, long long in_dist, long long out_dist,
                    void *stream);
+/* kfg_exec_batch for callers that may not allocate device memory while they
+ * transform (code inside a custom allocator or memory-pool hook, real-time
+ * loops with memory fixed at start-up).  It has no counterpart in the
+ * reference, whose transforms run on the host.  Complex 1-D plans and device
+ * pointers only.  Scratch of two-pass plans (batch * nfft complex elements)
+ * comes from one fixed device array per device of KFG_NOALLOC_SCRATCH_BYTES;
+ * a larger batch fails with KFG_EINVAL.  Calls that may overlap on the GPU
+ * (other streams or threads) race on that array: issue them on one stream.
+ * The first call on a device looks the array up (and may load the module
+ * holding it): make it before any stream capture.  Run-time specialised
+ * kernels are not used. */
+#define KFG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+int kfg_exec_batch_noalloc(kfg_plan *p, const void *in, void *out, long long batch, long long in_dist,
+                           long long out_dist, void *stream);
 /* Whole-signal filter: y receives nx - ntaps + 1 samples (the valid
  * convolution); *ny_out gets that count. */
 int kfg_fir_filter(kfg_plan *p, const float *x, size_t nx, float *y, size_t *ny_out, void *stream);

@@ -1033,3 +1033,17 @@ int kfg_batch_info(const kfg_batch* b, long long* out, int nout) {
 }
 
 }  // extern "C"
+
+// Internal hooks for kf_noalloc.cu (not exported): the schedule of a complex
+// 1-D batch, the thread's error message, the pointer test and the stream pick.
+namespace kf {
+__attribute__((visibility("hidden"))) int c2c_schedule(kfg_plan* p, long long batch, long long in_dist,
+                                                       long long out_dist, Schedule& s) {
+    if (!p || p->kind != K_C2C) return fail(KFG_EINVAL, "needs a complex 1-D plan (kfg_plan_c2c)");
+    size_t ib = 0, ob = 0;
+    return build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
+}
+__attribute__((visibility("hidden"))) int set_error(int code, const std::string& msg) { return fail(code, msg); }
+__attribute__((visibility("hidden"))) bool device_pointer(const void* ptr) { return is_device_ptr(ptr); }
+__attribute__((visibility("hidden"))) cudaStream_t stream_or_default(void* stream) { return pick(stream); }
+}  // namespace kf
