@@ -54,3 +54,48 @@ def to_complex128(a, dtype):
     if is_fixed(dtype):
         return a[..., 0].astype(np.float64) + 1j * a[..., 1].astype(np.float64)
     return a.astype(np.complex128)
+
+
+# ------------------------------------------------------------ uneven mix
+MIX_KINDS = ((0.6, "c2c", "float"), (0.9, "r2c", "float"), (1.0, "c2c", "int16_t"))
+
+
+def _smooth(lo, hi, primes):
+    out = {1}
+    for p in primes:
+        grown = set()
+        for v in out:
+            while v <= hi:
+                grown.add(v)
+                v *= p
+        out = grown
+    return sorted(v for v in out if lo <= v <= hi)
+
+
+def uneven_mix(count, seed=3, lo=16, hi=131072):
+    """Requests (kind, dtype, nfft) of the batched uneven-size mix.
+
+    nfft is drawn log-uniform on [lo, hi] and moved to the nearest (in log)
+    length of its class: 80% 2^a*3^b*5^c, 20% with at least one prime factor
+    7..31 (and none above 31).  Kinds: 60% complex float32, 30% real float32
+    (even nfft), 10% complex Q15.
+    """
+    rng = np.random.default_rng(seed)
+    smooth = np.array(_smooth(lo, hi, (2, 3, 5)))
+    s31 = set(_smooth(lo, hi, (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31)))
+    rough = np.array(sorted(s31 - set(smooth.tolist())))
+    pools = {}
+    for name, arr in (("smooth", smooth), ("rough", rough)):
+        pools[(name, False)] = arr
+        pools[(name, True)] = arr[arr % 2 == 0]
+    logs = {k: np.log(v) for k, v in pools.items()}
+    out = []
+    for _ in range(count):
+        u = rng.random()
+        kind, dtype = next((k, d) for c, k, d in MIX_KINDS if u < c)
+        target = np.log(lo) + rng.random() * (np.log(hi) - np.log(lo))
+        cls = "smooth" if rng.random() < 0.8 else "rough"
+        key = (cls, kind == "r2c")
+        n = int(pools[key][int(np.argmin(np.abs(logs[key] - target)))])
+        out.append((kind, dtype, n))
+    return out
