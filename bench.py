@@ -18,6 +18,8 @@ Printed JSON line (one, on rank 0):
           launch / its CUDA-event launch time) against the measured HBM peak
   cpu_baseline  the CPU restatement of the reference path (oracle/, OpenMP
           over transforms) on this host's cores, on a bounded sample
+  batched_mix  the uneven-size mix (20,000 requests) as one batch replayed
+          from a CUDA graph against the plain per-call form
 
 --impl reference times that CPU path on the same workload instead.
 """
@@ -215,6 +217,9 @@ def run_gpu(args):
         for i in range(len(us)):
             if not torch.equal(hout[i], ys[i].cpu()):
                 raise RuntimeError("e2e output differs from device output for %s" % (us[i],))
+    mix = None
+    if not args.no_mix:
+        mix = run_mix(args)
     cpu = None
     if not args.no_cpu:
         from oracle import kfo
@@ -224,7 +229,128 @@ def run_gpu(args):
                "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs)}
     return {"value": value, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e, "clocks": clocks, "cpu": cpu,
             "gpu_launches": args.steps * sum(launches_per_unit), "alg_bytes": alg_bytes,
-            "prepare_s": round(t_prep, 2)}
+            "prepare_s": round(t_prep, 2), "mix": mix}
+
+
+# ------------------------------------------------------------------ uneven mix
+MIX_COUNT = 20000
+
+
+def run_mix(args, count=MIX_COUNT):
+    """Batched uneven-size mix (20,000 requests, seed 3; uneven_mix in
+    tests/golden/inputs.py): one kfg_batch of all requests in two arenas, its launch shape
+    (threads per tile) picked by timing the candidates, captured in a CUDA
+    graph and replayed, against the plain per-call form (one kfg_exec_batch
+    per request, precompiled kernels) on the same arenas.  Returns GB/s of
+    compulsory bytes (input + output of every request) for both forms."""
+    import ctypes
+
+    import torch
+
+    import inputs
+    import kissfft_gb300 as kf
+
+    L = kf.core()
+    vp, ll, ci = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int
+    L.kfg_batch_create.restype = vp
+    L.kfg_batch_add.argtypes = [vp, ci, ci, ci, ll, ll]
+    L.kfg_batch_commit.argtypes = [vp, vp, vp, ci]
+    for fn in ("kfg_batch_run", "kfg_batch_capture", "kfg_batch_run_percall"):
+        getattr(L, fn).argtypes = [vp, vp]
+    L.kfg_batch_info.argtypes = [vp, vp, ci]
+    L.kfg_batch_free.argtypes = [vp]
+    kf.set_specialize(False)  # thousands of distinct plans: precompiled kernels in both forms
+    mix = inputs.uneven_mix(count, seed=3)
+    kinds = {"c2c": 1, "r2c": 2}
+    dts = {"float": 0, "int16_t": 2}
+    reqs, io, oo = [], 0, 0
+    for kind, d, n in mix:
+        esz = ESZ[d]
+        ib = n * esz if kind == "c2c" else n * 4
+        ob = n * esz if kind == "c2c" else (n // 2 + 1) * 8
+        reqs.append((kinds[kind], dts[d], n, io, oo, ib, ob))
+        io = (io + ib + 255) // 256 * 256
+        oo = (oo + ob + 255) // 256 * 256
+    alg = sum(r[5] + r[6] for r in reqs)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    ind = (torch.rand(io // 4, device="cuda", generator=gen) * 2 - 1).view(torch.uint8)  # uniform[-1, 1)
+    q15 = torch.zeros(io, dtype=torch.bool, device="cuda")
+    for r in reqs:
+        if r[1] == 2:
+            q15[r[3]:r[3] + r[5]] = True
+    ind[q15] = torch.randint(0, 256, (int(q15.sum()),), dtype=torch.uint8, device="cuda", generator=gen)
+    outd = torch.zeros(oo, dtype=torch.uint8, device="cuda")
+    st = vp(torch.cuda.current_stream().cuda_stream)
+    stream = torch.cuda.current_stream()
+
+    def commit(target):
+        B = L.kfg_batch_create()
+        for r in reqs:
+            if L.kfg_batch_add(B, r[0], r[1], r[2], r[3], r[4]) != 0:
+                raise RuntimeError(L.kfg_last_error().decode())
+        if L.kfg_batch_commit(B, vp(ind.data_ptr()), vp(outd.data_ptr()), target) != 0:
+            raise RuntimeError(L.kfg_last_error().decode())
+        return B
+
+    def timed(fn, steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    t_commit = time.perf_counter()
+    best = None
+    for target in (128, 256, 512):  # autotune: threads per tile the launches are widened towards
+        B = commit(target)
+        L.kfg_batch_run(B, st)
+        ms = timed(lambda: L.kfg_batch_run(B, st), 3)
+        if best is None or ms < best[1]:
+            if best is not None:
+                L.kfg_batch_free(best[0])
+            best = (B, ms, target)
+        else:
+            L.kfg_batch_free(B)
+    B, _, target = best
+    t_commit = time.perf_counter() - t_commit
+    info = (ctypes.c_longlong * 4)()
+    L.kfg_batch_info(B, info, 4)
+    direct_ms = timed(lambda: L.kfg_batch_run(B, st), max(3, args.steps // 3))
+    if L.kfg_batch_capture(B, st) != 0:
+        raise RuntimeError(L.kfg_last_error().decode())
+    for _ in range(args.warmup):
+        L.kfg_batch_run(B, st)
+    graph_ms = timed(lambda: L.kfg_batch_run(B, st), max(3, args.steps))
+    got = outd.clone()
+    L.kfg_batch_run_percall(B, st)  # warm-up
+    percall_ms = timed(lambda: L.kfg_batch_run_percall(B, st), 3)
+    ref = outd
+    # equal accuracy: both forms give the same transforms (Q15 bit for bit)
+    worst = 0.0
+    for r in reqs:
+        a, b = got[r[4]:r[4] + r[6]], ref[r[4]:r[4] + r[6]]
+        if r[1] == 2:
+            if not torch.equal(a, b):
+                raise RuntimeError("batched Q15 result differs from the per-call form (nfft %d)" % r[2])
+        else:
+            av, bv = a.view(torch.float32).double(), b.view(torch.float32).double()
+            worst = max(worst, float((av - bv).norm() / bv.norm().clamp_min(1e-30)))
+    L.kfg_batch_free(B)
+    distinct = len(set((r[0], r[1], r[2]) for r in reqs))
+    return {"workload": "uneven mix: %d requests, nfft log-uniform [16, 131072], 80%% 2^a3^b5^c / 20%% with a "
+                        "prime 7..31; 60%% c2c f32, 30%% r2c f32, 10%% c2c Q15; seed 3" % count,
+            "requests": count, "distinct_plans": distinct, "compulsory_bytes": alg,
+            "graph": {"ms": round(graph_ms, 3), "gbs": round(alg / graph_ms / 1e6, 1)},
+            "direct": {"ms": round(direct_ms, 3), "gbs": round(alg / direct_ms / 1e6, 1)},
+            "percall": {"ms": round(percall_ms, 3), "gbs": round(alg / percall_ms / 1e6, 1)},
+            "speedup_vs_percall": round(percall_ms / graph_ms, 2),
+            "autotuned_target_threads": target, "launches": int(info[2]), "tiles": int(info[3]),
+            "max_rel_diff_vs_percall": worst, "commit_and_tune_s": round(t_commit, 2)}
 
 
 # ------------------------------------------------------------------ CPU arm
@@ -258,6 +384,7 @@ def main():
                     help="CPU baseline of the GPU arm: minimum seconds of CPU work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mix", action="store_true", help="skip the batched uneven-mix measurement")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch of the dominant kernel from an ncu capture")
     ap.add_argument("--specialize", type=int, default=1,
@@ -274,7 +401,7 @@ def main():
         for c in args.case:
             dt, n, b = c.split(":")
             _CASES.append((dt, int(n), int(b)))
-        args.no_e2e = args.no_cpu = True
+        args.no_e2e = args.no_cpu = args.no_mix = True
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     config = {"workload": "mixed-radix complex forward: nfft 480,1000,3003,65536 x float32,Q15,Q31, "
@@ -313,6 +440,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
                 "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
+                "batched_mix": r["mix"],
                 "kernels": ("plan-specialised (NVRTC)" if args.specialize else "precompiled families") +
                 ("; autotuned" if args.autotune else "") + "; set-up before warm-up %.1f s" % r["prepare_s"]}
         print(json.dumps(line))

@@ -21,6 +21,8 @@
 #define KF_MAXJ 64
 #define KF_MAXO 32
 #define KF_MAXT 512
+// real split / merge elements per work item of a batched element launch
+#define KF_ELEM_CHUNK 2048
 
 namespace kf {
 

@@ -240,4 +240,30 @@ __global__ void __launch_bounds__(256) kf_merge_kernel(const __grid_constant__ K
         merge_item<S>(a, it);
 }
 
+// Real split / merge items of many two-pass real plans in one launch
+// (batched requests): work item w covers elements [w.tile * KF_ELEM_CHUNK,
+// (w.tile + 1) * KF_ELEM_CHUNK) of step w.step.  KIND 1 splits, 2 merges.
+template <typename S, int KIND>
+__global__ void __launch_bounds__(256) kf_multi_elem_kernel(const __grid_constant__ MultiArgs m) {
+    __shared__ unsigned long long s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(m.counter, 1ull);
+        __syncthreads();
+        const unsigned long long it = s_item;
+        __syncthreads();  // all threads hold the item before thread 0 takes the next
+        if (it >= (unsigned long long)m.nitems) break;
+        const MultiItem w = m.items[it];
+        const KArgs& a = m.steps[w.step];
+        const long long total = a.G * (a.sub[0].L / 2 + 1);
+        const long long lo = w.tile * KF_ELEM_CHUNK;
+        const long long hi = lo + KF_ELEM_CHUNK < total ? lo + KF_ELEM_CHUNK : total;
+        for (long long e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+            if constexpr (KIND == 1)
+                split_item<S>(a, e);
+            else
+                merge_item<S>(a, e);
+        }
+    }
+}
+
 }  // namespace kf

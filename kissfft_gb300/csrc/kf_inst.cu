@@ -71,6 +71,20 @@ cudaError_t KF_NAME(launch_multi_dt, KF_INST_DT, _fam, KF_INST_FAM)(int mode, co
 cudaError_t KF_NAME(launch_elem_dt, KF_INST_DT, , )(const Step& st, cudaStream_t s) {
     return launch_elem<kf_inst_s>(st, s);
 }
+
+cudaError_t KF_NAME(launch_multi_elem_dt, KF_INST_DT, , )(int kind, const MultiArgs& m, cudaStream_t s) {
+    typedef kf_inst_s S;
+    const void* k = kind == 1 ? (const void*)kf_multi_elem_kernel<S, 1> : (const void*)kf_multi_elem_kernel<S, 2>;
+    int per = 0, nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, 0) != cudaSuccess || per < 1) per = 1;
+    long long grid = (long long)per * (nsm > 0 ? nsm : 1);
+    if (grid > m.nitems) grid = m.nitems;
+    if (grid <= 0) return cudaSuccess;
+    void* args[] = {(void*)&m};
+    return cudaLaunchKernel(k, dim3((unsigned)grid), dim3(256), args, 0, s);
+}
 #endif
 
 }  // namespace kf

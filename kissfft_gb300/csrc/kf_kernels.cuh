@@ -65,7 +65,8 @@ static cudaError_t launch_elem(const Step& st, cudaStream_t s) {
     cudaError_t launch_engine_dt##D##_fam0(const Step&, cudaStream_t); \
     cudaError_t launch_engine_dt##D##_fam1(const Step&, cudaStream_t); \
     cudaError_t launch_engine_dt##D##_fam2(const Step&, cudaStream_t); \
-    cudaError_t launch_elem_dt##D(const Step&, cudaStream_t);
+    cudaError_t launch_elem_dt##D(const Step&, cudaStream_t);           \
+    cudaError_t launch_multi_elem_dt##D(int, const MultiArgs&, cudaStream_t);
 KF_DECL_DT(0)
 KF_DECL_DT(1)
 KF_DECL_DT(2)
@@ -96,6 +97,17 @@ inline cudaError_t launch_multi(int dtype, int fam, int mode, const MultiArgs& m
         KF_CASE_MULTI(3)
     }
 #undef KF_CASE_MULTI
+    return cudaErrorInvalidValue;
+}
+
+// kind 1: real split, 2: real merge items of many steps (kf_multi_elem_kernel)
+inline cudaError_t launch_multi_elem(int dtype, int kind, const MultiArgs& m, cudaStream_t s) {
+    switch (dtype) {
+        case 0: return launch_multi_elem_dt0(kind, m, s);
+        case 1: return launch_multi_elem_dt1(kind, m, s);
+        case 2: return launch_multi_elem_dt2(kind, m, s);
+        case 3: return launch_multi_elem_dt3(kind, m, s);
+    }
     return cudaErrorInvalidValue;
 }
 

@@ -772,11 +772,16 @@ struct kfg_batch {
     };
     struct Launch {
         int phase = 0, dtype = 0, mode = 0, fam = 0, T = 32, smem = 0;
-        int elem_step = -1;  // >= 0: a split/merge element step launched on its own
+        int elem_kind = 0;  // 0: engine tiles; 1 / 2: real split / merge elements
+        double cost = 0;
         std::vector<MultiItem> items;
         MultiItem* d_items = nullptr;
         unsigned long long* d_counter = nullptr;
     };
+    // launches of one phase are independent: they run on several streams
+    static constexpr int kAux = 3;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork = nullptr, join[kAux] = {};
     std::vector<Req> reqs;
     void* in_arena = nullptr;
     void* out_arena = nullptr;
@@ -802,7 +807,14 @@ struct kfg_batch {
         d_steps = nullptr;
         committed = false;
     }
-    ~kfg_batch() { release(); }
+    ~kfg_batch() {
+        release();
+        for (int k = 0; k < kAux; ++k) {
+            if (aux[k]) cudaStreamDestroy(aux[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
+    }
 };
 
 namespace {
@@ -876,19 +888,24 @@ int batch_commit(kfg_batch* b) {
             phase_of.push_back(ph++);
         }
     }
-    // launches: (phase, dtype, mode, family, tile class); element steps alone
+    // launches: engine tiles keyed by (phase, dtype, mode, family, threads
+    // class, shared-memory class), so that small tiles are not run with the
+    // block shape of the largest; split / merge elements keyed by (phase,
+    // dtype, kind)
+    auto pow2_ceil = [](long long v) {
+        long long c = 1;
+        while (c < v) c <<= 1;
+        return c;
+    };
     std::map<std::string, int> lkey;
     for (size_t i = 0; i < b->steps.size(); ++i) {
         const Step& st = b->steps[i];
-        if (st.kind != 0) {
-            kfg_batch::Launch L;
-            L.phase = phase_of[i];
-            L.elem_step = (int)i;
-            b->launches.push_back(L);
-            continue;
-        }
         std::ostringstream k;
-        k << phase_of[i] << ":" << st.dtype << ":" << st.mode << ":" << st.fam << ":" << (st.cfg.smem > 64 * 1024);
+        if (st.kind != 0)
+            k << "E" << phase_of[i] << ":" << st.dtype << ":" << st.kind;
+        else
+            k << phase_of[i] << ":" << st.dtype << ":" << st.mode << ":" << st.fam << ":" << pow2_ceil(st.cfg.T) << ":"
+              << pow2_ceil(std::max(st.cfg.smem, 8192));
         auto it = lkey.find(k.str());
         int li;
         if (it == lkey.end()) {
@@ -899,11 +916,18 @@ int batch_commit(kfg_batch* b) {
             L.dtype = st.dtype;
             L.mode = st.mode;
             L.fam = st.fam;
+            L.elem_kind = st.kind;
             b->launches.push_back(L);
         } else {
             li = it->second;
         }
         auto& L = b->launches[li];
+        if (st.kind != 0) {
+            const long long total = st.args.G * (st.args.sub[0].L / 2 + 1);
+            for (long long c = 0; c * KF_ELEM_CHUNK < total; ++c) L.items.push_back(MultiItem{(int)i, 0, c});
+            L.cost += (double)total;
+            continue;
+        }
         L.T = std::max(L.T, st.cfg.T);
         L.smem = std::max(L.smem, st.cfg.smem);
         for (long long t = 0; t < st.args.ntiles; ++t) L.items.push_back(MultiItem{(int)i, 0, t});
@@ -916,16 +940,26 @@ int batch_commit(kfg_batch* b) {
         cost[i] = st.cfg.J * L * (L > 1 ? std::log2(L) : 1.0);
     }
     for (auto& L : b->launches) {
-        std::stable_sort(L.items.begin(), L.items.end(),
-                         [&](const MultiItem& a, const MultiItem& c) { return cost[a.step] > cost[c.step]; });
+        if (L.elem_kind == 0) {
+            std::stable_sort(L.items.begin(), L.items.end(),
+                             [&](const MultiItem& a, const MultiItem& c) { return cost[a.step] > cost[c.step]; });
+            for (auto& w : L.items) L.cost += cost[w.step];
+        }
         L.d_items = upload(b, L.items);
         void* c = nullptr;
         if (cudaMalloc(&c, sizeof(unsigned long long)) != cudaSuccess) return fail(KFG_ENOMEM, "kfg_batch: counter");
         b->allocs.push_back(c);
         L.d_counter = (unsigned long long*)c;
     }
-    std::stable_sort(b->launches.begin(), b->launches.end(),
-                     [](const kfg_batch::Launch& a, const kfg_batch::Launch& c) { return a.phase < c.phase; });
+    // by phase; inside a phase the most expensive launch first
+    std::stable_sort(b->launches.begin(), b->launches.end(), [](const kfg_batch::Launch& a, const kfg_batch::Launch& c) {
+        return a.phase != c.phase ? a.phase < c.phase : a.cost > c.cost;
+    });
+    for (int k = 0; k < kfg_batch::kAux; ++k) {
+        if (!b->aux[k]) KFG_CK(cudaStreamCreateWithFlags(&b->aux[k], cudaStreamNonBlocking));
+        if (!b->join[k]) KFG_CK(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+    }
+    if (!b->fork) KFG_CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     std::vector<KArgs> ka;
     for (auto& st : b->steps) ka.push_back(st.args);
     b->d_steps = upload(b, ka);
@@ -933,21 +967,41 @@ int batch_commit(kfg_batch* b) {
     return KFG_OK;
 }
 
+cudaError_t batch_launch(kfg_batch* b, const kfg_batch::Launch& L, cudaStream_t strm) {
+    cudaError_t e = cudaMemsetAsync(L.d_counter, 0, sizeof(unsigned long long), strm);
+    if (e != cudaSuccess) return e;
+    MultiArgs m;
+    m.steps = b->d_steps;
+    m.items = L.d_items;
+    m.nitems = (long long)L.items.size();
+    m.counter = L.d_counter;
+    if (L.elem_kind != 0) return launch_multi_elem(L.dtype, L.elem_kind, m, strm);
+    return launch_multi(L.dtype, L.fam, L.mode, m, L.T, L.smem, 0, strm);
+}
+
+// Phases run in order on strm; the launches of one phase fork onto the
+// auxiliary streams and join back before the next phase.
 int batch_enqueue(kfg_batch* b, cudaStream_t strm) {
-    for (auto& L : b->launches) {
-        cudaError_t e;
-        if (L.elem_step >= 0) {
-            e = launch_step(b->steps[L.elem_step], strm);
-        } else {
-            cudaMemsetAsync(L.d_counter, 0, sizeof(unsigned long long), strm);
-            MultiArgs m;
-            m.steps = b->d_steps;
-            m.items = L.d_items;
-            m.nitems = (long long)L.items.size();
-            m.counter = L.d_counter;
-            e = launch_multi(L.dtype, L.fam, L.mode, m, L.T, L.smem, 0, strm);
+    size_t i = 0;
+    while (i < b->launches.size()) {
+        size_t j = i;
+        while (j < b->launches.size() && b->launches[j].phase == b->launches[i].phase) ++j;
+        const int naux = (int)std::min<size_t>(j - i - 1, kfg_batch::kAux);
+        if (naux > 0) {
+            KFG_CK(cudaEventRecord(b->fork, strm));
+            for (int k = 0; k < naux; ++k) KFG_CK(cudaStreamWaitEvent(b->aux[k], b->fork, 0));
         }
-        if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("kfg_batch launch: ") + cudaGetErrorString(e));
+        for (size_t l = i; l < j; ++l) {
+            const int lane = (int)((l - i) % (size_t)(naux + 1));
+            cudaStream_t s = lane == 0 ? strm : b->aux[lane - 1];
+            cudaError_t e = batch_launch(b, b->launches[l], s);
+            if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("kfg_batch launch: ") + cudaGetErrorString(e));
+        }
+        for (int k = 0; k < naux; ++k) {
+            KFG_CK(cudaEventRecord(b->join[k], b->aux[k]));
+            KFG_CK(cudaStreamWaitEvent(strm, b->join[k], 0));
+        }
+        i = j;
     }
     return KFG_OK;
 }
