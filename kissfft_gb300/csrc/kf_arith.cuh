@@ -92,6 +92,19 @@ struct ArFixed {
         c.i = sround((P)c.i * (P)s);
         return c;
     }
+    // C_MUL(t, a, w) then C_ADDTO(acc, t) of kf_bfly_generic, with acc kept as
+    // an untruncated word: truncation to S commutes with the wrapping adds, so
+    // the caller truncates once after the whole sum.  Twiddles have
+    // |w| <= SMAX, so -w.i fits S and every product is one widening
+    // multiply-add; the sums are exact in P (|a*w| < 2^(2*FB)).
+    static KF_HD void cmul_acc(W& ar, W& ai, C a, C w) {
+        const P rnd = (P)1 << (FB - 1);
+        const S nwi = (S)(0 - w.i);
+        const P re = (P)a.r * (P)w.r + (P)a.i * (P)nwi + rnd;
+        const P im = (P)a.r * (P)w.i + (P)a.i * (P)w.r + rnd;
+        ar = add(ar, (W)(re >> FB));
+        ai = add(ai, (W)(im >> FB));
+    }
 };
 
 template <>

@@ -342,12 +342,9 @@ KF_HD void group2(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
 //
 // Fixed point follows kf_bfly_generic (kiss_fft.c:192-233) exactly: output
 // leg q1 sums legs q = 0..P-1 in order, each product rounded, with twiddle
-// index (q*fstride*k) mod N, k = u + q1*m.  Since fstride*m = N/P that index
-// is (q*fstride*u + ((q*q1) mod P)*N/P) mod N; for u == 0 (every group of a
-// leaf stage) it takes only the P values r*N/P, so those are loaded once and
-// the fully unrolled sums index them by constants.  That unrolled form is
-// kept to P <= 13: its code grows as P^2, and P = 17..31 (rare leaf radices)
-// would multiply the compile time of every kernel that can meet them.
+// index (q*fstride*k) mod N, k = u + q1*m.  Those P-1 twiddles of every
+// (u, q1) are one row of the stage's compact table (kf_shape.h gen_row),
+// read with vector loads; the sum is kept untruncated until the store.
 //
 // IEEE types (no bit-exactness to keep, only the error bound) multiply the
 // legs by tw[q*fstride*u] first and then take the size-P DFT on the table's
@@ -376,40 +373,27 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     if (dst_g) go = gout<S, MODE>(t, g.job, g.pos0);
     C y[P];
     if constexpr (kFixed) {
-        if constexpr (P <= 13) {
-            if (u == 0) {
-                C W[P];
-#pragma unroll
-                for (int r = 0; r < P; ++r) W[r] = KF_LDG(tw + r * NP);
-#pragma unroll
-                for (int q1 = 0; q1 < P; ++q1) {
-                    C acc = x[0];
-#pragma unroll
-                    for (int q = 1; q < P; ++q) acc = c_add(acc, Arr::cmul(x[q], W[(q * q1) % P]));
-                    if (dst_g)
-                        go.st(q1 * sa.mloc, acc);
-                    else
-                        t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
-                }
-                return;
-            }
-        }
+        typedef typename Arr::W W;
+        constexpr int RP = gen_row(P);
+        const C* row = (const C*)tb.tw_stage + sa.tw_off + (long long)u * P * RP;
 #pragma unroll 1
         for (int q1 = 0; q1 < P; ++q1) {
-            const int step = sa.fs * (u + q1 * sa.m);
-            int twidx = 0;
-            C acc = x[0];
+            C w[RP];
+            ldro_vec<S, RP>(row + q1 * RP, w);
+            W ar = x[0].r, ai = x[0].i;
 #pragma unroll
-            for (int q = 1; q < P; ++q) {
-                twidx += step;
-                if (twidx >= N) twidx -= N;
-                acc = c_add(acc, Arr::cmul(x[q], KF_LDG(tw + twidx)));
-            }
+            for (int q = 1; q < P; ++q) Arr::cmul_acc(ar, ai, x[q], w[q - 1]);
+            C acc;
+            acc.r = Arr::st(ar);
+            acc.i = Arr::st(ai);
             if (dst_g)
                 go.st(q1 * sa.mloc, acc);
             else
                 t.sst(g.A0 + q1 * sa.iloc, g.job, acc);
         }
+        (void)tw;
+        (void)N;
+        (void)NP;
         return;
     } else {
         constexpr int h = (P - 1) / 2;

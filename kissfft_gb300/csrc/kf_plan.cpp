@@ -125,6 +125,22 @@ bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
     for (int j = 0; j < si.K; ++j) {
         const int p = si.radix[j];
         if (si.twoff[j] < 0) continue;
+        if (p > 5) {
+            // generic-radix rows (kf_shape.h gen_row)
+            const int RP = gen_row(p);
+            const long long fs = si.fs[j], m = si.m[j];
+            uint8_t* base = tws.data() + (size_t)si.twoff[j] * esz;
+            for (long long u = 0; u < m; ++u)
+                for (int q1 = 0; q1 < p; ++q1) {
+                    const long long step = fs * (u + q1 * m) % n;
+                    long long idx = 0;
+                    for (int q = 1; q < p; ++q) {
+                        idx = (idx + step) % n;
+                        memcpy(base + (size_t)((u * p + q1) * RP + (q - 1)) * esz, twf.data() + (size_t)idx * esz, esz);
+                    }
+                }
+            continue;
+        }
         const int W = tw_width(p);
         uint8_t* base = tws.data() + (size_t)si.twoff[j] * esz;
         for (int u = 0; u < si.m[j]; ++u)

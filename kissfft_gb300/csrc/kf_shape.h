@@ -22,7 +22,7 @@ struct ShapeInfo {
     int radix[KF_MAXST];
     int m[KF_MAXST];
     int fs[KF_MAXST];
-    int twoff[KF_MAXST];  // -1 for generic-radix stages (they read the full table)
+    int twoff[KF_MAXST];  // -1 for stages that read the full table (IEEE generic radix, p > 31)
     long long tw_count;   // entries of the compact per-stage table
     int nsub, split;
     int rev_total;        // ints of all reverse tables
@@ -43,6 +43,12 @@ KF_CX int tw_width(int p) { return p == 2 ? 1 : (p == 3 ? 2 : 4); }
 KF_CX bool small_prime(int p) {
     return p == 7 || p == 11 || p == 13 || p == 17 || p == 19 || p == 23 || p == 29 || p == 31;
 }
+
+// Fixed-point generic-radix stages (p = 7..31) read their twiddles from
+// rows: for every u < m and output leg q1 < p, gen_row(p) consecutive
+// entries tw[(q*fstride*(u + q1*m)) mod N] for q = 1..p-1 (then padding) --
+// the exact sequence kf_bfly_generic walks (kiss_fft.c:218-226).
+KF_CX int gen_row(int p) { return (p - 1 + 3) & ~3; }
 
 // magic multiplier M with n / d == (n * M) >> 40 for n * d < 2^40
 KF_CX unsigned long long div_magic(int d) {
@@ -158,6 +164,10 @@ KF_CX ShapeInfo make_shape(int dtype, int n, int inverse, int lmax, int real_nff
             cnt = (cnt + 3) & ~3LL;  // 4-entry alignment for vector loads
             si.twoff[j] = (int)cnt;
             cnt += (long long)tw_width(f[j]) * si.m[j] + 2;
+        } else if ((dtype == KF_Q15 || dtype == KF_Q31) && small_prime(f[j])) {
+            cnt = (cnt + 3) & ~3LL;
+            si.twoff[j] = (int)cnt;
+            cnt += (long long)gen_row(f[j]) * f[j] * si.m[j];
         } else {
             si.twoff[j] = -1;
         }
