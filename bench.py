@@ -173,14 +173,22 @@ def run_gpu(args):
     ms = t0.elapsed_time(t1) / args.steps
     alg_bytes = sum(2 * n * ESZ[dt] * b for dt, n, b in us)
     value = alg_bytes / (ms * 1e-3) / 1e9
-    # per-unit launch times (same workload, events between launches)
-    ev = [[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)] for _ in us]
+    # per-unit launch times: each unit launched back to back between two
+    # events (the device never waits for the host inside the bracket), every
+    # launch re-reading its >L2 input from HBM
     per = [0.0] * len(us)
-    for _ in range(max(1, args.steps)):
-        step(ev)
+    reps = max(3, args.steps)
+    for i, (dt, n, b) in enumerate(us):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        for i in range(len(us)):
-            per[i] += ev[i][0].elapsed_time(ev[i][1]) / max(1, args.steps)
+        kf.kiss_fft_batch(cfgs[i], xs[i], ys[i], b)  # keeps the device busy while the bracket is queued
+        e0.record(stream)
+        for _ in range(reps):
+            kf.kiss_fft_batch(cfgs[i], xs[i], ys[i], b)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per[i] = e0.elapsed_time(e1) / reps
     unit_rows = []
     for i, (dt, n, b) in enumerate(us):
         byts = 2 * n * ESZ[dt] * b

@@ -23,6 +23,15 @@
 
 namespace kf {
 
+// float samples (the only type whose plans use three-stage register groups)
+template <typename S>
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+__host__ __device__
+#endif
+constexpr bool is_f32() {
+    return sizeof(S) == 4 && (S)0.5 != (S)0;
+}
+
 template <typename S>
 struct alignas(2 * sizeof(S)) cpx {
     S r, i;

@@ -44,7 +44,7 @@ __device__ __forceinline__ bool kf_mbar_wait(unsigned bar, unsigned parity) {
     return false;
 }
 
-template <typename S, int MODE, unsigned KM>
+template <typename S, int MODE, kmask_t KM>
 struct DevExec {
     // TMA staging: thread 0 re-arms the staging buffer once the first pass
     // has read it (next >= 0: the tile to fetch)
@@ -94,7 +94,7 @@ struct DevExec {
 // through tiles blockIdx.x, blockIdx.x + gridDim.x, ... of J jobs each; the
 // tile lives in dynamic shared memory.  JF/CIF/COF > 0 fix the tile shape at
 // compile time (specialised kernels); 0 takes it from the arguments.
-template <typename S, int MODE, unsigned KM, int JF = 0, int CIF = -1, int COF = -1>
+template <typename S, int MODE, kmask_t KM, int JF = 0, int CIF = -1, int COF = -1>
 __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, const KSub& s1) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
@@ -125,7 +125,7 @@ __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, cons
 // Tiles of contiguous input (a.tma): persistent CTAs, the next tile's input
 // is bulk-copied into a staging buffer while the current tile runs its
 // passes; the first pass reads the staged tile through shared memory.
-template <typename S, int MODE, unsigned KM, int JF = 0>
+template <typename S, int MODE, kmask_t KM, int JF = 0>
 __device__ __forceinline__ void engine_body_tma(const KArgs& a, const KSub& s0) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
@@ -182,18 +182,18 @@ template <typename S, int MODE, int FAM>
 __global__ void __launch_bounds__(KF_MAXT) kf_engine_kernel(const __grid_constant__ KArgs a) {
     if constexpr (MODE == MODE_C2C || MODE == MODE_R2C) {
         if (a.tma) {
-            engine_body_tma<S, MODE, family_mask(FAM)>(a, a.sub[0]);
+            engine_body_tma<S, MODE, family_mask(FAM, is_f32<S>())>(a, a.sub[0]);
             return;
         }
     }
-    engine_body<S, MODE, family_mask(FAM)>(a, a.sub[0], a.sub[1]);
+    engine_body<S, MODE, family_mask(FAM, is_f32<S>())>(a, a.sub[0], a.sub[1]);
 }
 
 // Persistent multi-plan kernel: tiles of many plans (one sample type and
 // mode) in one launch, pulled from a work queue.  Every step's shape is read
 // from its KArgs in global memory; blockDim and the shared tile are sized
 // for the largest step of the launch.
-template <typename S, int MODE, unsigned KM>
+template <typename S, int MODE, kmask_t KM>
 __global__ void __launch_bounds__(KF_MAXT) kf_multi_kernel(const __grid_constant__ MultiArgs m) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];

@@ -338,6 +338,77 @@ KF_HD void group2(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     }
 }
 
+// Three stages: stage a+2 (radix PC), then a+1 (PB), then a (PA); element
+// (ea, eb, ec) at register k = ea + PA*(eb + PB*ec).  Stage s of the group
+// takes the twiddle row of u = (sum of the deeper group digits * their mloc
+// + ul) * m_low + U, as in group2.
+template <typename S, int MODE, int PA, int PB, int PC>
+KF_HD void group3(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, const GroupIx& g, int U,
+                  bool src_g, bool dst_g) {
+    typedef cpx<S> C;
+    const KStage& sa = sb.st[ps.a];
+    const KStage& sbb = sb.st[ps.a + 1];
+    const KStage& sc = sb.st[ps.a + 2];
+    C x[PA * PB * PC];
+    if (src_g) {
+        const GIn<S, MODE> gi = gin<S, MODE>(t, g.job, g.A0);
+#pragma unroll
+        for (int ec = 0; ec < PC; ++ec)
+#pragma unroll
+            for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+                for (int ea = 0; ea < PA; ++ea)
+                    x[ea + PA * (eb + PB * ec)] = gi.ld(ea * sa.iloc + eb * sbb.iloc + ec * sc.iloc);
+    } else {
+#pragma unroll
+        for (int ec = 0; ec < PC; ++ec)
+#pragma unroll
+            for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+                for (int ea = 0; ea < PA; ++ea)
+                    x[ea + PA * (eb + PB * ec)] = t.sld(g.A0 + ea * sa.iloc + eb * sbb.iloc + ec * sc.iloc, g.job);
+    }
+    {
+        C w[PC - 1], c0, c1;
+        stage_tw<S, PC>(tb, sc, g.ul * sb.m_low + U, w, c0, c1);
+#pragma unroll
+        for (int k = 0; k < PA * PB; ++k) bfly<S, PC, PA * PB>(x + k, w, c0, c1, sb.inverse != 0);
+    }
+#pragma unroll
+    for (int ec = 0; ec < PC; ++ec) {
+        C w[PB - 1], c0, c1;
+        stage_tw<S, PB>(tb, sbb, (ec * sc.mloc + g.ul) * sb.m_low + U, w, c0, c1);
+#pragma unroll
+        for (int ea = 0; ea < PA; ++ea) bfly<S, PB, PA>(x + ea + PA * PB * ec, w, c0, c1, sb.inverse != 0);
+    }
+#pragma unroll
+    for (int ec = 0; ec < PC; ++ec)
+#pragma unroll
+        for (int eb = 0; eb < PB; ++eb) {
+            C w[PA - 1], c0, c1;
+            stage_tw<S, PA>(tb, sa, (eb * sbb.mloc + ec * sc.mloc + g.ul) * sb.m_low + U, w, c0, c1);
+            bfly<S, PA, 1>(x + PA * (eb + PB * ec), w, c0, c1, sb.inverse != 0);
+        }
+    if (dst_g) {
+        const GOut<S, MODE> go = gout<S, MODE>(t, g.job, g.pos0);
+#pragma unroll
+        for (int ec = 0; ec < PC; ++ec)
+#pragma unroll
+            for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+                for (int ea = 0; ea < PA; ++ea)
+                    go.st(ea * sa.mloc + eb * sbb.mloc + ec * sc.mloc, x[ea + PA * (eb + PB * ec)]);
+    } else {
+#pragma unroll
+        for (int ec = 0; ec < PC; ++ec)
+#pragma unroll
+            for (int eb = 0; eb < PB; ++eb)
+#pragma unroll
+                for (int ea = 0; ea < PA; ++ea)
+                    t.sst(g.A0 + ea * sa.iloc + eb * sbb.iloc + ec * sc.iloc, g.job, x[ea + PA * (eb + PB * ec)]);
+    }
+}
+
 // Generic radix P (a prime 7..31) on registers.
 //
 // Fixed point follows kf_bfly_generic (kiss_fft.c:192-233) exactly: output
@@ -512,8 +583,8 @@ KF_HD void rtg_store(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPa
 // is the mask of pass kinds compiled in (kind_bit): a family kernel covers
 // a family of plans, a specialised kernel exactly its own passes.  kf_factor
 // emits 4s, at most one 2, then 3s, 5s and larger primes, so only 9 ordered
-// radix pairs can occur.
-template <typename S, int MODE, unsigned KM>
+// radix pairs and 12 ordered triples (up to 64 elements) can occur.
+template <typename S, int MODE, kmask_t KM>
 KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass& ps, bool is_last, int tid, int T,
                     bool src_g, bool dst_g) {
     const int NG = t.J * ps.H * ps.ML;
@@ -531,6 +602,11 @@ KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPas
         if constexpr ((KM & kind_bit(10 * PA + PB)) != 0)                                   \
             group2<S, MODE, PA, PB>(t, sb, tb, ps, g, U, src_g, dst_g);                     \
         break;
+#define KF_G3(PA, PB, PC)                                                                   \
+    case 1000 + 100 * PA + 10 * PB + PC:                                                    \
+        if constexpr ((KM & kind_bit(1000 + 100 * PA + 10 * PB + PC)) != 0)                \
+            group3<S, MODE, PA, PB, PC>(t, sb, tb, ps, g, U, src_g, dst_g);                 \
+        break;
 #define KF_GG(P)                                                                            \
     case 100 + P:                                                                           \
         if constexpr ((KM & kind_bit(100 + P)) != 0) groupg<S, MODE, P>(t, sb, tb, ps, g, U, src_g, dst_g); \
@@ -539,6 +615,9 @@ KF_HD void run_pass(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPas
             KF_G1(3) KF_G1(5)
             KF_G2(2, 3) KF_G2(2, 5) KF_G2(3, 3) KF_G2(3, 5) KF_G2(4, 3) KF_G2(4, 5) KF_G2(5, 5)
             KF_GG(7) KF_GG(11) KF_GG(13) KF_GG(17) KF_GG(19) KF_GG(23) KF_GG(29) KF_GG(31)
+            KF_G3(4, 4, 4) KF_G3(4, 4, 2) KF_G3(4, 4, 3) KF_G3(4, 2, 3) KF_G3(4, 2, 5) KF_G3(4, 3, 3)
+            KF_G3(4, 3, 5) KF_G3(2, 3, 3) KF_G3(2, 3, 5) KF_G3(2, 5, 5) KF_G3(3, 3, 3) KF_G3(3, 3, 5)
+#undef KF_G3
 #undef KF_G1
 #undef KF_G2
 #undef KF_GG

@@ -40,7 +40,7 @@ cudaError_t KF_NAME(launch_engine_dt, KF_INST_DT, _fam, KF_INST_FAM)(const Step&
 cudaError_t KF_NAME(launch_multi_dt, KF_INST_DT, _fam, KF_INST_FAM)(int mode, const MultiArgs& m, int T, int smem,
                                                                      long long grid, cudaStream_t s) {
     typedef kf_inst_s S;
-    constexpr unsigned KM = family_mask(KF_INST_FAM);
+    constexpr kmask_t KM = family_mask(KF_INST_FAM, KF_INST_DT == 0);
     const void* k = nullptr;
     switch (mode) {
         case MODE_C2C: k = (const void*)kf_multi_kernel<S, MODE_C2C, KM>; break;

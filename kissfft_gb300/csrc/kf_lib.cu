@@ -109,7 +109,7 @@ struct kfg_plan {
     void* d_H = nullptr;
     // autotuned launch shapes per (batch, in_dist, out_dist): J, minb, tma per step
     std::mutex tune_mu;
-    std::map<std::string, std::vector<std::array<int, 3>>> tuned;
+    std::map<std::string, std::vector<std::array<int, 4>>> tuned;
     ~kfg_plan() {
         if (d_H) cudaFree(d_H);
     }
@@ -269,12 +269,13 @@ std::string tune_key(long long batch, long long in_dist, long long out_dist) {
     return o.str();
 }
 
-void apply_cfgs(Schedule& s, const std::vector<std::array<int, 3>>& v) {
+void apply_cfgs(Schedule& s, const std::vector<std::array<int, 4>>& v) {
     size_t k = 0;
     for (auto& st : s.steps) {
         if (st.kind != 0) continue;
         if (k >= v.size()) break;
         const auto& c = v[k++];
+        if (c[3] && !st.args.col_in) recolumn_step(st);
         if (c[0] != st.cfg.J) reshape_step(st, c[0]);
         st.cfg.minb = c[1];
         st.tma_ok = c[2];
@@ -299,7 +300,7 @@ std::string plan_sig(const kfg_plan* p) {
         snprintf(name, sizeof(name), "%s", prop.name);
     for (char* c = name; *c; ++c)
         if (*c == ' ') *c = '_';
-    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0);
+    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v2";
     return o.str();
 }
 
@@ -315,7 +316,7 @@ std::string tune_file() {
     return d + "/tune.txt";
 }
 
-bool tune_load(const std::string& key, std::vector<std::array<int, 3>>& v) {
+bool tune_load(const std::string& key, std::vector<std::array<int, 4>>& v) {
     std::ifstream f(tune_file());
     std::string line;
     bool found = false;
@@ -323,16 +324,16 @@ bool tune_load(const std::string& key, std::vector<std::array<int, 3>>& v) {
         size_t sp = line.find(' ');
         if (sp == std::string::npos || line.compare(0, sp, key) != 0 || sp != key.size()) continue;
         std::istringstream is(line.substr(sp + 1));
-        std::vector<std::array<int, 3>> r;
-        std::array<int, 3> c;
-        while (is >> c[0] >> c[1] >> c[2]) r.push_back(c);
+        std::vector<std::array<int, 4>> r;
+        std::array<int, 4> c;
+        while (is >> c[0] >> c[1] >> c[2] >> c[3]) r.push_back(c);
         v = r;
         found = true;  // the last line for a key wins
     }
     return found;
 }
 
-void tune_store(const std::string& key, const std::vector<std::array<int, 3>>& v) {
+void tune_store(const std::string& key, const std::vector<std::array<int, 4>>& v) {
     std::string path = tune_file();
     std::string dir = path.substr(0, path.rfind('/'));
     std::string cmd;
@@ -340,7 +341,7 @@ void tune_store(const std::string& key, const std::vector<std::array<int, 3>>& v
         if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
     std::ofstream f(path, std::ios::app);
     f << key;
-    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2];
+    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2] << " " << c[3];
     f << "\n";
 }
 
@@ -608,7 +609,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
     if (!p || batch < 1 || p->kind == K_FIR) return fail(KFG_EINVAL, "kfg_autotune: bad arguments");
     const std::string key = tune_key(batch, in_dist, out_dist);
     const std::string dkey = plan_sig(p) + ":" + key;
-    std::vector<std::array<int, 3>> best;
+    std::vector<std::array<int, 4>> best;
     if (tune_load(dkey, best)) {
         std::lock_guard<std::mutex> lk(p->tune_mu);
         p->tuned[key] = best;
@@ -637,17 +638,25 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
         if (st0.kind != 0) continue;
         std::vector<Step> cands;
         const int J0 = st0.cfg.J;
-        for (int J : {J0 / 2, J0, J0 * 2, J0 * 4}) {
-            Step c = st0;
-            if (J < 1 || (J != J0 && !reshape_step(c, J))) continue;
-            const int m0 = c.cfg.minb;
-            for (int mb : {1, m0, m0 + 1}) {
-                bool dup = false;
-                for (auto& d : cands) dup |= (d.cfg.J == c.cfg.J && d.cfg.minb == mb);
-                if (dup) continue;
-                Step cm = c;
-                cm.cfg.minb = mb;
-                cands.push_back(cm);
+        // row-mode steps also try column-layout tiles with 2..8 jobs
+        Step colst = st0;
+        const bool can_col = recolumn_step(colst);
+        for (int col = 0; col <= (can_col ? 1 : 0); ++col) {
+            const Step& base = col ? colst : st0;
+            const std::vector<int> Js = col ? std::vector<int>{2, 4, 8} : std::vector<int>{J0 / 2, J0, J0 * 2, J0 * 4};
+            for (int J : Js) {
+                Step c = base;
+                if (J < 1 || (J != base.cfg.J && !reshape_step(c, J))) continue;
+                const int m0 = c.cfg.minb;
+                for (int mb : {1, m0, m0 + 1}) {
+                    bool dup = false;
+                    for (auto& d : cands)
+                        dup |= (d.cfg.J == c.cfg.J && d.cfg.minb == mb && d.args.col_in == c.args.col_in);
+                    if (dup) continue;
+                    Step cm = c;
+                    cm.cfg.minb = mb;
+                    cands.push_back(cm);
+                }
             }
         }
         if (specialize_enabled()) {
@@ -661,7 +670,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
             for (auto& t : th) t.join();
         }
         float bt = -1.f;
-        std::array<int, 3> bc = {st0.cfg.J, st0.cfg.minb, 1};
+        std::array<int, 4> bc = {st0.cfg.J, st0.cfg.minb, 1, st0.args.col_in};
         for (auto& c : cands) {
             for (int tma = 1; tma >= 0; --tma) {
                 Step x = c;
@@ -669,7 +678,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
                 float ms = time_step(x, roles, strm, e0, e1, 3);
                 if (ms > 0 && (bt < 0 || ms < bt)) {
                     bt = ms;
-                    bc = {c.cfg.J, c.cfg.minb, tma};
+                    bc = {c.cfg.J, c.cfg.minb, tma, c.args.col_in};
                 }
                 if (!x.args.tma) break;  // staging not eligible: one timing is enough
             }
@@ -677,7 +686,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
         best.push_back(bc);
         // later steps read what this one wrote: run it once with the winner
         Step w = st0;
-        std::vector<std::array<int, 3>> one = {bc};
+        std::vector<std::array<int, 4>> one = {bc};
         Schedule tmp;
         tmp.steps.push_back(w);
         apply_cfgs(tmp, one);

@@ -302,6 +302,18 @@ bool enable_tma(Step& st, const void* in) {
     return true;
 }
 
+// Column-layout tiles (jobs fastest in shared memory and in the group
+// order) for a row-mode engine step: fewer bank conflicts for strides that
+// the swizzle does not spread, at the price of shorter global runs (32/J
+// elements of each job per warp access).
+bool recolumn_step(Step& st) {
+    if (st.kind != 0 || st.mode == MODE_FIR || st.args.col_in || st.args.col_out) return false;
+    st.cfg.col_in = st.cfg.col_out = 1;
+    st.args.col_in = st.args.col_out = 1;
+    st.args.tma = 0;
+    return true;
+}
+
 static int default_minb(int T, int smem) {
     const int by_threads = 2048 / std::max(T, 32);
     const int by_smem = (227 * 1024) / std::max(smem + 1024, 1);

@@ -78,6 +78,7 @@ int sub_family(const KSub& sb);
 // room for the staging buffer.  Returns whether staging was switched on.
 struct Step;
 bool enable_tma(Step& st, const void* in);
+bool recolumn_step(Step& st);
 void set_tma_enabled(int on);
 bool tma_enabled();
 

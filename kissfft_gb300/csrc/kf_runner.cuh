@@ -12,7 +12,7 @@ namespace kf {
 #if defined(__CUDACC__)
 #pragma nv_exec_check_disable
 #endif
-template <typename S, int MODE, unsigned KM, class X>
+template <typename S, int MODE, kmask_t KM, class X>
 KF_HD void run_sub(X& x, Tile<S>& t, const KSub& sb, const KTab& tb, bool src_first, bool dst_last, int col_in,
                    int col_out) {
 #pragma unroll
@@ -41,7 +41,7 @@ KF_HD void run_sub(X& x, Tile<S>& t, const KSub& sb, const KTab& tb, bool src_fi
 #if defined(__CUDACC__)
 #pragma nv_exec_check_disable
 #endif
-template <typename S, int MODE, unsigned KM, class X>
+template <typename S, int MODE, kmask_t KM, class X>
 KF_HD void run_tile(X& x, const KArgs& a, const KSub& s0, const KSub& s1, Tile<S>& t, int ci, int co) {
     if constexpr (MODE == MODE_C2R) {
         t.col = ci;

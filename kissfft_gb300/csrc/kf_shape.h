@@ -84,7 +84,8 @@ KF_CX int factor_into(int n, int* f) {
 
 // One sub-plan over global stages [g0, g1); reverse tables are appended at
 // *rev_next (ints).
-KF_CX void shape_sub(ShapeInfo& si, KSub& sb, int n, int inverse, int g0, int g1, int pair_rmax, int& rev_next) {
+KF_CX void shape_sub(ShapeInfo& si, KSub& sb, int n, int inverse, int g0, int g1, int pair_rmax, int trip_rmax,
+                     int& rev_next) {
     const int nst = g1 - g0;
     sb.N = n;
     sb.nst = nst;
@@ -103,27 +104,50 @@ KF_CX void shape_sub(ShapeInfo& si, KSub& sb, int n, int inverse, int g0, int g1
         sb.st[i].mloc = si.m[j] / sb.m_low;
         sb.st[i].iloc = si.fs[j] / si.fs[g0];
     }
-    // passes in execution order: from the leaf stage down to stage 0;
-    // adjacent radices 2..5 share a register group
+    // passes in execution order: from the leaf stage down to stage 0.
+    // Adjacent radices 2..5 share a register group of up to three stages;
+    // the grouping minimises the number of passes, then the largest group.
+    // bpass/bmaxr/bns[i]: best grouping of stages 0..i-1 and its last group.
+    int bpass[KF_MAXST + 1]{}, bmaxr[KF_MAXST + 1]{}, bns[KF_MAXST + 1]{};
+    for (int i = 1; i <= nst; ++i) {
+        bpass[i] = 1 << 20;
+        for (int ns = 3; ns >= 1; --ns) {  // ties: the larger group on the leaf side
+            if (ns > i) continue;
+            int R = 1;
+            bool ok = true;
+            for (int k = i - ns; k < i; ++k) {
+                const int pk = sb.st[k].p;
+                if (ns > 1 && (pk < 2 || pk > 5)) ok = false;
+                R *= pk;
+            }
+            if (!ok || (ns == 2 && R > pair_rmax) || (ns == 3 && R > trip_rmax)) continue;
+            const int np1 = bpass[i - ns] + 1;
+            const int mr = bmaxr[i - ns] > R ? bmaxr[i - ns] : R;
+            if (np1 < bpass[i] || (np1 == bpass[i] && mr < bmaxr[i])) {
+                bpass[i] = np1;
+                bmaxr[i] = mr;
+                bns[i] = ns;
+            }
+        }
+    }
     int np = 0, i = nst - 1;
     while (i >= 0) {
         KPass p{};
-        const int pa = sb.st[i].p;
-        const int pb = i >= 1 ? sb.st[i - 1].p : 0;
-        if (i >= 1 && pa >= 2 && pa <= 5 && pb >= 2 && pb <= 5 && pa * pb <= pair_rmax) {
-            p.a = i - 1;
-            p.ns = 2;
-            p.kind = 10 * pb + pa;
-            p.R = pa * pb;
-            i -= 2;
+        const int ns = bns[i + 1];
+        p.a = i - ns + 1;
+        p.ns = ns;
+        p.R = 1;
+        for (int k = p.a; k <= i; ++k) p.R *= sb.st[k].p;
+        if (ns == 3) {
+            p.kind = 1000 + 100 * sb.st[p.a].p + 10 * sb.st[p.a + 1].p + sb.st[p.a + 2].p;
+        } else if (ns == 2) {
+            p.kind = 10 * sb.st[p.a].p + sb.st[p.a + 1].p;
         } else {
             // p == 1 only for nfft == 1: the reference's p = 1 generic butterfly
-            p.a = i;
-            p.ns = 1;
+            const int pa = sb.st[i].p;
             p.kind = (pa >= 2 && pa <= 5) ? pa : (small_prime(pa) ? 100 + pa : KIND_RT_GENERIC);
-            p.R = pa;
-            i -= 1;
         }
+        i -= ns;
         const int b = p.a + p.ns - 1;
         p.H = sb.st[p.a].iloc;
         p.ML = sb.st[b].mloc;
@@ -174,11 +198,12 @@ KF_CX ShapeInfo make_shape(int dtype, int n, int inverse, int lmax, int real_nff
     }
     si.tw_count = cnt;
     const int prm = dtype == KF_F64 ? 16 : 25;
+    const int trm = dtype == KF_F32 ? 48 : 0;  // three-stage register groups: float only
     int rev_next = 0;
     if (n <= lmax) {
         si.nsub = 1;
         si.split = 0;
-        shape_sub(si, si.sub[0], n, inverse, 0, K, prm, rev_next);
+        shape_sub(si, si.sub[0], n, inverse, 0, K, prm, trm, rev_next);
     } else {
         int best = -1;
         long long bestv = 0, P = 1;
@@ -196,8 +221,8 @@ KF_CX ShapeInfo make_shape(int dtype, int n, int inverse, int lmax, int real_nff
         }
         si.nsub = 2;
         si.split = best;
-        shape_sub(si, si.sub[0], n, inverse, best, K, prm, rev_next);
-        shape_sub(si, si.sub[1], n, inverse, 0, best, prm, rev_next);
+        shape_sub(si, si.sub[0], n, inverse, best, K, prm, trm, rev_next);
+        shape_sub(si, si.sub[1], n, inverse, 0, best, prm, trm, rev_next);
     }
     for (int s = 0; s < si.nsub; ++s) {
         for (int k = 0; k < si.sub[s].npass; ++k)
@@ -213,53 +238,74 @@ KF_CX ShapeInfo make_shape(int dtype, int n, int inverse, int lmax, int real_nff
 }
 
 // Bit of a pass kind in a kernel's kind mask (the pass kinds it compiles).
-KF_CX unsigned kind_bit(int kind) {
+typedef unsigned long long kmask_t;
+KF_CX kmask_t kind_bit(int kind) {
     switch (kind) {
-        case 2: return 1u << 0;
-        case 4: return 1u << 1;
-        case 42: return 1u << 2;
-        case 44: return 1u << 3;
-        case 3: return 1u << 4;
-        case 5: return 1u << 5;
-        case 23: return 1u << 6;
-        case 25: return 1u << 7;
-        case 33: return 1u << 8;
-        case 35: return 1u << 9;
-        case 43: return 1u << 10;
-        case 45: return 1u << 11;
-        case 55: return 1u << 12;
-        case 107: return 1u << 13;
-        case 111: return 1u << 14;
-        case 113: return 1u << 15;
-        case 117: return 1u << 16;
-        case 119: return 1u << 17;
-        case 123: return 1u << 18;
-        case 129: return 1u << 19;
-        case 131: return 1u << 20;
-        case KIND_RT_GENERIC: return 1u << 21;
+        case 2: return 1ull << 0;
+        case 4: return 1ull << 1;
+        case 42: return 1ull << 2;
+        case 44: return 1ull << 3;
+        case 3: return 1ull << 4;
+        case 5: return 1ull << 5;
+        case 23: return 1ull << 6;
+        case 25: return 1ull << 7;
+        case 33: return 1ull << 8;
+        case 35: return 1ull << 9;
+        case 43: return 1ull << 10;
+        case 45: return 1ull << 11;
+        case 55: return 1ull << 12;
+        case 107: return 1ull << 13;
+        case 111: return 1ull << 14;
+        case 113: return 1ull << 15;
+        case 117: return 1ull << 16;
+        case 119: return 1ull << 17;
+        case 123: return 1ull << 18;
+        case 129: return 1ull << 19;
+        case 131: return 1ull << 20;
+        case KIND_RT_GENERIC: return 1ull << 21;
+        // three-stage groups (radices of stages a, a+1, a+2), float plans only
+        case 1444: return 1ull << 22;
+        case 1442: return 1ull << 23;
+        case 1443: return 1ull << 24;
+        case 1423: return 1ull << 25;
+        case 1425: return 1ull << 26;
+        case 1433: return 1ull << 27;
+        case 1435: return 1ull << 28;
+        case 1233: return 1ull << 29;
+        case 1235: return 1ull << 30;
+        case 1255: return 1ull << 31;
+        case 1333: return 1ull << 32;
+        case 1335: return 1ull << 33;
     }
     return 0;
 }
-constexpr unsigned KM_POW2 = 0xfu;        // kinds 2, 4, 42, 44
-constexpr unsigned KM_SMOOTH = 0x1fffu;   // + 3, 5 and the 2/3/5 pairs
-constexpr unsigned KM_GENERAL = 0x3fffffu;  // + generic primes 7..31 and any p
-constexpr unsigned KM_RTG = 1u << 21;
+constexpr kmask_t KM_POW2 = 0xfull;           // kinds 2, 4, 42, 44
+constexpr kmask_t KM_SMOOTH = 0x1fffull;      // + 3, 5 and the 2/3/5 pairs
+constexpr kmask_t KM_GENERAL = 0x3fffffull;   // + generic primes 7..31 and any p
+constexpr kmask_t KM_RTG = 1ull << 21;
+constexpr kmask_t KM_TRIP_POW2 = (1ull << 22) | (1ull << 23);  // 444, 442
+constexpr kmask_t KM_TRIP = 0xfffull << 22;                     // all twelve triples
 
-KF_CX unsigned kind_mask(const KSub& sb) {
-    unsigned m = 0;
+KF_CX kmask_t kind_mask(const KSub& sb) {
+    kmask_t m = 0;
     for (int k = 0; k < sb.npass; ++k) m |= kind_bit(sb.ps[k].kind);
     return m;
 }
 
-KF_CX unsigned family_mask(int fam) { return fam == FAM_POW2 ? KM_POW2 : (fam == FAM_SMOOTH ? KM_SMOOTH : KM_GENERAL); }
+// Pass kinds a family kernel compiles; triples only where plans have them.
+KF_CX kmask_t family_mask(int fam, bool f32) {
+    const kmask_t m = fam == FAM_POW2 ? KM_POW2 : (fam == FAM_SMOOTH ? KM_SMOOTH : KM_GENERAL);
+    if (!f32) return m;
+    return m | (fam == FAM_POW2 ? KM_TRIP_POW2 : KM_TRIP);
+}
 
 // Smallest kernel family whose compiled pass kinds cover a sub-plan.
 KF_CX int family_of(const KSub& sb) {
     int f = FAM_POW2;
     for (int k = 0; k < sb.npass; ++k) {
         const int kd = sb.ps[k].kind;
-        if (kd == 2 || kd == 4 || kd == 42 || kd == 44) continue;
-        if (kd < 99)
+        if (kd == 2 || kd == 4 || kd == 42 || kd == 44 || kd == 1444 || kd == 1442) continue;
+        if (kd < 99 || kd > 1000)
             f = f > FAM_SMOOTH ? f : FAM_SMOOTH;
         else
             f = FAM_GENERAL;

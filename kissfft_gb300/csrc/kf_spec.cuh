@@ -19,7 +19,7 @@ template <typename S, int MODE, int DT, int N, int INV, int LMAX, int SUB, int J
           int MINB>
 __global__ void __launch_bounds__(T, MINB) kf_spec_kernel(const __grid_constant__ KArgs a) {
     static_assert(kSpecShape<DT, N, INV, LMAX>.error == 0, "plan shape");
-    constexpr unsigned KM = kind_mask(kSpecShape<DT, N, INV, LMAX>.sub[SUB]);
+    constexpr kmask_t KM = kind_mask(kSpecShape<DT, N, INV, LMAX>.sub[SUB]);
     if constexpr ((MODE == MODE_C2C || MODE == MODE_R2C) && COLIN == 0 && COLOUT == 0) {
         if (a.tma) {
             engine_body_tma<S, MODE, KM, J>(a, kSpecShape<DT, N, INV, LMAX>.sub[SUB]);

@@ -15,9 +15,9 @@
 
 using namespace kf;
 
-static int g_force_J = 0, g_force_T = 0;
+static int g_force_J = 0, g_force_T = 0, g_force_col = 0;
 
-template <typename S, int MODE, unsigned KM>
+template <typename S, int MODE, kmask_t KM>
 struct CpuExec {
     int T;
     void sync() {}
@@ -64,11 +64,11 @@ static int run_engine_step_f(const Step& st) {
     t.lim_in = lin;
     t.lim_out = lout;
     t.err = &err;
-    CpuExec<S, MODE, family_mask(FAM)> x;
+    CpuExec<S, MODE, family_mask(FAM, is_f32<S>())> x;
     x.T = c.T;
     for (long long tile = 0; tile < a.ntiles; ++tile) {
         for (int j = 0; j < a.J; ++j) job_entry(a, tile, a.J, j, inb[j], outb[j], U[j], lin[j], lout[j]);
-        run_tile<S, MODE, family_mask(FAM)>(x, a, a.sub[0], a.sub[1], t, a.col_in, a.col_out);
+        run_tile<S, MODE, family_mask(FAM, is_f32<S>())>(x, a, a.sub[0], a.sub[1], t, a.col_in, a.col_out);
     }
     return err;
 }
@@ -122,6 +122,10 @@ static int run_schedule(Schedule& s, const void* in, void* out, const void* firH
             st.cfg.T = std::max(st.cfg.T, cfg_min_threads(st.args.sub[0], st.mode, g_force_J));
         }
         if (g_force_T && st.kind == 0) st.cfg.T = std::max(g_force_T, cfg_min_threads(st.args.sub[0], st.mode, st.cfg.J));
+        if (g_force_col && st.kind == 0 && st.mode != MODE_FIR) {
+            st.cfg.col_in = st.cfg.col_out = 1;
+            st.args.col_in = st.args.col_out = 1;
+        }
         int e = 0;
         switch (st.dtype) {
             case KF_F32: e = run_step_t<float>(st); break;
@@ -140,6 +144,9 @@ void emu_force(int J, int T) {
     g_force_J = J;
     g_force_T = T;
 }
+
+// column-layout tiles (jobs fastest) for every engine step
+void emu_force_col(int col) { g_force_col = col; }
 
 int emu_c2c(int dtype, int n, int inverse, int lmax, const void* in, void* out, long long batch, long long in_dist,
             long long in_stride, long long out_dist) {

@@ -151,3 +151,37 @@ def test_forced_tile_shapes(emu):
                 assert np.array_equal(y, kfo.fft(x, 0, "int16_t")), (J, T, n)
         finally:
             emu.emu_force(0, 0)
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
+def test_column_tiles_on_row_batches(emu, dtype):
+    """Column-layout tiles (jobs fastest in shared memory) on row-major
+    batches give the same results as row-layout tiles."""
+    emu.emu_force_col(1)
+    try:
+        for J in (2, 8):
+            emu.emu_force(J, 0)
+            for n in (30, 480, 1000, 3003, 1024, 65536):
+                for inv in (0, 1):
+                    x = inputs.cpx((11, n), dtype, n + J + inv)
+                    y = np.zeros_like(x)
+                    rc = emu.emu_c2c(DT[dtype], n, inv, 0, p(x), p(y), L(11), L(n), L(1), L(n))
+                    assert rc == 0
+                    check(y, lambda: kfo.fft(x, inv, dtype), x, dtype, n, inv)
+            for nfft in (480, 4096, 6006):
+                t = inputs.real((5, nfft), dtype, nfft)
+                f = kfo.empty_cpx((5, nfft // 2 + 1), dtype)
+                assert emu.emu_r2c(DT[dtype], nfft, 0, p(t), p(f), L(5)) == 0
+                g = inputs.cpx((5, nfft // 2 + 1), dtype, nfft + 1)
+                t2 = np.zeros((5, nfft), kfo.SCALAR[dtype])
+                assert emu.emu_c2r(DT[dtype], nfft, 0, p(g), p(t2), L(5)) == 0
+                if fixed(dtype):
+                    assert np.array_equal(f, kfo.fftr(t, dtype)), (J, nfft)
+                    assert np.array_equal(t2, kfo.fftri(g, nfft, dtype)), (J, nfft)
+                else:
+                    ex = np.fft.rfft(t.astype(np.float64), axis=-1)
+                    e = np.max(np.linalg.norm(f - ex, axis=-1) / np.linalg.norm(ex, axis=-1))
+                    assert e <= 2e-7 * np.log2(nfft), (J, nfft, e)
+    finally:
+        emu.emu_force_col(0)
+        emu.emu_force(0, 0)
