@@ -147,6 +147,75 @@ int kfg_batch_run_percall(kfg_batch *b, void *stream);
 int kfg_batch_info(const kfg_batch *b, long long *out, int nout);
 void kfg_batch_free(kfg_batch *b);
 
+/* Serving loop (the served form of the path): requests submitted from any
+ * host thread are admitted in arrival order under an HBM budget, batched
+ * continuously (everything admitted since the last launch goes out together,
+ * up to KFG_SERVE_SLOTS batches in flight on their own streams), and
+ * completed asynchronously.  Plans and fast-FIR responses stay cached on the
+ * device.  Buffers may be device, pinned host (moved by one zero-copy
+ * gather/scatter kernel per batch) or ordinary host memory, and must stay
+ * valid until the request is waited for.  Latency = completion - submit. */
+#define KFG_SERVE_C2C 1    /* kiss_fft:   n0 points, dtype, inverse        */
+#define KFG_SERVE_R2C 2    /* kiss_fftr:  n0 reals -> n0/2+1 bins          */
+#define KFG_SERVE_C2R 3    /* kiss_fftri: n0/2+1 bins -> n0 reals          */
+#define KFG_SERVE_C2C_2D 4 /* kiss_fftnd: n0 x n1 complex, row-major       */
+#define KFG_SERVE_FIR 5    /* kiss_fastfir: n0 float taps, len samples in,
+                              len - n0 + 1 samples out (valid part)       */
+#define KFG_SERVE_SLOTS 8
+typedef struct {
+    int kind, dtype, inverse;
+    int n0, n1;
+    long long len;
+    const float *taps;
+    const void *in;
+    void *out;
+} kfg_serve_req;
+typedef struct {
+    long long completed, failed, batches, max_batch, peak_hbm_bytes;
+    double p50_s, p99_s, max_s, mean_s; /* latency, submit to completion */
+    double req_per_s, gbs, bytes;       /* over first submit .. last completion */
+} kfg_serve_stats;
+typedef struct kfg_server kfg_server;
+/* hbm_budget: bytes (0 = 40 GiB); slots: batches in flight (0 = 4) */
+kfg_server *kfg_server_create(size_t hbm_budget, int slots);
+/* returns a request id > 0, or a negative KFG_E* code */
+long long kfg_server_submit(kfg_server *s, const kfg_serve_req *req);
+/* timeout_s < 0 waits without limit; returns the request's status, or 1 on
+ * timeout (the request stays pending and may be waited for again) */
+int kfg_server_wait(kfg_server *s, long long id, double timeout_s, double *latency_s);
+int kfg_server_drain(kfg_server *s); /* waits for every submitted request */
+int kfg_server_stats(kfg_server *s, kfg_serve_stats *out);
+int kfg_server_reset_stats(kfg_server *s);
+void kfg_server_free(kfg_server *s);
+
+/* Synthetic load for the serving loop: Poisson arrivals at `rate` requests/s
+ * for `seconds` (rate <= 0: `count` requests submitted at once), kinds drawn
+ * with weights mix[] = {c2c, r2c, 2-D, fast FIR} (float), c2c/r2c lengths
+ * log-uniform [c2c_min, c2c_max] moved to the next fast size, 2-D sides
+ * log-uniform [d2_min, d2_max], FIR taps log-uniform [fir_taps_min,
+ * fir_taps_max] N(0,1) (16 filters) on signals of log-uniform
+ * [fir_len_min, fir_len_max] samples.  Inputs are N(0,1) in a pinned pool.
+ * Then the first percall_max requests run again through the plain per-call
+ * form (one synchronous kfg_exec / kfg_fir_filter each). */
+typedef struct {
+    double rate, seconds;
+    long long count;
+    unsigned long long seed;
+    double mix[4];
+    int c2c_min, c2c_max, d2_min, d2_max, fir_taps_min, fir_taps_max;
+    long long fir_len_min, fir_len_max;
+    long long percall_max;
+    int in_pool_mb, out_pool_mb;
+} kfg_loadtest;
+typedef struct {
+    long long offered;
+    double submit_s;
+    kfg_serve_stats served;
+    long long percall_count;
+    double percall_req_per_s, percall_gbs, percall_p50_s, percall_p99_s;
+} kfg_loadtest_result;
+int kfg_server_loadtest(kfg_server *s, const kfg_loadtest *cfg, kfg_loadtest_result *res);
+
 /* Plan introspection for tests and tools: out[0] = transform kind, out[1] =
  * dtype, out[2] = length, out[3] = number of HBM passes of a 1-D plan,
  * out[4] = kernel family, out[5] = tile length. */

@@ -375,3 +375,131 @@ def plan_info(cfg):
     plan_ptr = ctypes.c_void_p.from_address(cfg.ptr + 40).value
     c.kfg_plan_info(ctypes.c_void_p(plan_ptr), out, 6)
     return tuple(int(v) for v in out)
+
+
+# ---------------------------------------------------------------- serving loop
+SERVE_C2C, SERVE_R2C, SERVE_C2R, SERVE_C2C_2D, SERVE_FIR = 1, 2, 3, 4, 5
+
+
+class ServeReq(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("dtype", ctypes.c_int), ("inverse", ctypes.c_int), ("n0", ctypes.c_int),
+                ("n1", ctypes.c_int), ("len", ctypes.c_longlong), ("taps", ctypes.c_void_p),
+                ("in_", ctypes.c_void_p), ("out", ctypes.c_void_p)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_longlong) for n in ("completed", "failed", "batches", "max_batch", "peak_hbm_bytes")] + \
+               [(n, ctypes.c_double) for n in ("p50_s", "p99_s", "max_s", "mean_s", "req_per_s", "gbs", "bytes")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class LoadTest(ctypes.Structure):
+    _fields_ = [("rate", ctypes.c_double), ("seconds", ctypes.c_double), ("count", ctypes.c_longlong),
+                ("seed", ctypes.c_ulonglong), ("mix", ctypes.c_double * 4)] + \
+               [(n, ctypes.c_int) for n in ("c2c_min", "c2c_max", "d2_min", "d2_max", "fir_taps_min",
+                                            "fir_taps_max")] + \
+               [("fir_len_min", ctypes.c_longlong), ("fir_len_max", ctypes.c_longlong),
+                ("percall_max", ctypes.c_longlong), ("in_pool_mb", ctypes.c_int), ("out_pool_mb", ctypes.c_int)]
+
+
+class LoadTestResult(ctypes.Structure):
+    _fields_ = [("offered", ctypes.c_longlong), ("submit_s", ctypes.c_double), ("served", ServeStats),
+                ("percall_count", ctypes.c_longlong)] + \
+               [(n, ctypes.c_double) for n in ("percall_req_per_s", "percall_gbs", "percall_p50_s", "percall_p99_s")]
+
+
+def _serve_lib():
+    L = core()
+    if not getattr(L, "_serve_ready", False):
+        vp, ll = ctypes.c_void_p, ctypes.c_longlong
+        L.kfg_server_create.restype = vp
+        L.kfg_server_create.argtypes = [ctypes.c_size_t, ctypes.c_int]
+        L.kfg_server_submit.restype = ll
+        L.kfg_server_submit.argtypes = [vp, ctypes.POINTER(ServeReq)]
+        L.kfg_server_wait.argtypes = [vp, ll, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+        L.kfg_server_drain.argtypes = [vp]
+        L.kfg_server_stats.argtypes = [vp, ctypes.POINTER(ServeStats)]
+        L.kfg_server_reset_stats.argtypes = [vp]
+        L.kfg_server_free.argtypes = [vp]
+        L.kfg_server_loadtest.argtypes = [vp, ctypes.POINTER(LoadTest), ctypes.POINTER(LoadTestResult)]
+        L._serve_ready = True
+    return L
+
+
+class Server(object):
+    """The serving loop (kfg_server_*): submit requests from any thread, wait
+    for them, read p50/p99 latency and throughput.  Buffers (numpy arrays,
+    torch tensors or raw addresses) must stay alive until waited for."""
+
+    def __init__(self, hbm_budget=0, slots=0):
+        self.L = _serve_lib()
+        self.ptr = self.L.kfg_server_create(int(hbm_budget), int(slots))
+        if not self.ptr:
+            raise KissFFTError("kfg_server_create: " + (self.L.kfg_last_error() or b"").decode())
+        self._keep = {}
+
+    def submit(self, kind, inp, out, n0, n1=0, dtype="float", inverse=0, taps=None, length=0):
+        r = ServeReq()
+        r.kind, r.dtype, r.inverse, r.n0, r.n1, r.len = kind, DTYPE_CODE[dtype], int(inverse), int(n0), int(n1), \
+            int(length)
+        r.taps = _ptr(taps)[0] if taps is not None else None
+        r.in_ = _ptr(inp)[0]
+        r.out = _ptr(out)[0]
+        rid = self.L.kfg_server_submit(ctypes.c_void_p(self.ptr), ctypes.byref(r))
+        if rid <= 0:
+            raise KissFFTError("kfg_server_submit: " + (self.L.kfg_last_error() or b"").decode())
+        self._keep[rid] = (inp, out, taps)
+        return rid
+
+    def wait(self, rid, timeout=-1.0):
+        lat = ctypes.c_double(0)
+        rc = self.L.kfg_server_wait(ctypes.c_void_p(self.ptr), ctypes.c_longlong(rid), float(timeout),
+                                    ctypes.byref(lat))
+        if rc == 1:
+            return None
+        self._keep.pop(rid, None)
+        if rc != 0:
+            raise KissFFTError("request %d failed (%d): %s" % (rid, rc, (self.L.kfg_last_error() or b"").decode()))
+        return lat.value
+
+    def drain(self):
+        self.L.kfg_server_drain(ctypes.c_void_p(self.ptr))
+
+    def stats(self):
+        st = ServeStats()
+        self.L.kfg_server_stats(ctypes.c_void_p(self.ptr), ctypes.byref(st))
+        return st.as_dict()
+
+    def loadtest(self, **kw):
+        cfg = LoadTest()
+        defaults = dict(rate=50000.0, seconds=5.0, count=0, seed=4, mix=(0.25, 0.25, 0.25, 0.25), c2c_min=64,
+                        c2c_max=65536, d2_min=256, d2_max=1024, fir_taps_min=255, fir_taps_max=4095,
+                        fir_len_min=1 << 16, fir_len_max=1 << 22, percall_max=2000, in_pool_mb=256,
+                        out_pool_mb=2048)
+        defaults.update(kw)
+        for k, v in defaults.items():
+            if k == "mix":
+                for i in range(4):
+                    cfg.mix[i] = v[i]
+            else:
+                setattr(cfg, k, v)
+        res = LoadTestResult()
+        rc = self.L.kfg_server_loadtest(ctypes.c_void_p(self.ptr), ctypes.byref(cfg), ctypes.byref(res))
+        if rc:
+            raise KissFFTError("loadtest: " + (self.L.kfg_last_error() or b"").decode())
+        out = {n: getattr(res, n) for n, _ in res._fields_ if n != "served"}
+        out["served"] = res.served.as_dict()
+        return out
+
+    def close(self):
+        if self.ptr:
+            self.L.kfg_server_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

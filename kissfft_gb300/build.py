@@ -116,6 +116,9 @@ def build(verbose=False, jobs=None):
     out = os.path.join(BUILD, "kf_lib.o")
     tasks.append(([NVCC] + NVFLAGS + ["-c", os.path.join(CSRC, "kf_lib.cu"), "-o", out],
                   [os.path.join(CSRC, "kf_lib.cu")] + hdrs, out))
+    out = os.path.join(BUILD, "kf_serve.o")
+    tasks.append(([NVCC] + NVFLAGS + ["-c", os.path.join(CSRC, "kf_serve.cu"), "-o", out],
+                  [os.path.join(CSRC, "kf_serve.cu")] + hdrs, out))
     out = os.path.join(BUILD, "kf_noalloc.o")
     tasks.append(([NVCC] + NVFLAGS + ["-c", os.path.join(CSRC, "kf_noalloc.cu"), "-o", out],
                   [os.path.join(CSRC, "kf_noalloc.cu")] + hdrs, out))
