@@ -20,6 +20,8 @@ Printed JSON line (one, on rank 0):
           over transforms) on this host's cores, on a bounded sample
   batched_mix  the uneven-size mix (20,000 requests) as one batch replayed
           from a CUDA graph against the plain per-call form
+  serving  the serving loop under Poisson arrivals: p50/p99 latency and
+          throughput, saturated throughput, and the per-call form
 
 --impl reference times that CPU path on the same workload instead.
 """
@@ -228,6 +230,9 @@ def run_gpu(args):
     mix = None
     if not args.no_mix:
         mix = run_mix(args)
+    serving = None
+    if not args.no_serve:
+        serving = run_serving(args)
     cpu = None
     if not args.no_cpu:
         from oracle import kfo
@@ -237,7 +242,7 @@ def run_gpu(args):
                "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs)}
     return {"value": value, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e, "clocks": clocks, "cpu": cpu,
             "gpu_launches": args.steps * sum(launches_per_unit), "alg_bytes": alg_bytes,
-            "prepare_s": round(t_prep, 2), "mix": mix}
+            "prepare_s": round(t_prep, 2), "mix": mix, "serving": serving}
 
 
 # ------------------------------------------------------------------ uneven mix
@@ -361,6 +366,42 @@ def run_mix(args, count=MIX_COUNT):
             "max_rel_diff_vs_percall": worst, "commit_and_tune_s": round(t_commit, 2)}
 
 
+# ------------------------------------------------------------------ serving loop
+def run_serving(args):
+    """Serving loop (kfg_server, 40 GB HBM budget): Poisson arrivals at
+    50,000 requests/s for 5 s of a mix of c2c (N log-uniform 64..65536),
+    r2c, 2-D (256..1024 per side) and fast-FIR (255..4095 taps, 2^16..2^22
+    samples) requests in equal shares (seed 4), inputs and outputs in pinned
+    host memory; then the same mix submitted all at once (the loop's
+    saturated throughput); then the first 2,000 requests through the plain
+    per-call form.  Latency is submit to completion, p50/p99."""
+    import kissfft_gb300 as kf
+
+    kf.set_specialize(False)
+    srv = kf.Server(hbm_budget=40 << 30, slots=4)
+    try:
+        poisson = srv.loadtest(rate=50000.0, seconds=5.0, seed=4, percall_max=2000)
+        sat = srv.loadtest(rate=0.0, count=20000, seed=5, percall_max=0)
+    finally:
+        srv.close()
+    ps, ss = poisson["served"], sat["served"]
+    return {"workload": "Poisson 50k req/s x 5 s; c2c/r2c N 64..65536, 2-D 256..1024 per side, fast FIR 255..4095 "
+                        "taps on 2^16..2^22 samples, equal shares, float32, pinned host buffers; seed 4; "
+                        "HBM budget 40 GB",
+            "offered": poisson["offered"], "completed": ps["completed"], "failed": ps["failed"],
+            "p50_ms": round(ps["p50_s"] * 1e3, 3), "p99_ms": round(ps["p99_s"] * 1e3, 3),
+            "req_per_s": round(ps["req_per_s"], 1), "gbs": round(ps["gbs"], 2), "batches": ps["batches"],
+            "host_busy_s": round(ps["host_s"], 3),
+            "peak_hbm_gb": round(ps["peak_hbm_bytes"] / 1e9, 3),
+            "saturated": {"requests": sat["offered"], "req_per_s": round(ss["req_per_s"], 1),
+                          "gbs": round(ss["gbs"], 2), "p50_ms": round(ss["p50_s"] * 1e3, 3),
+                          "p99_ms": round(ss["p99_s"] * 1e3, 3), "host_busy_s": round(ss["host_s"], 3)},
+            "percall": {"requests": poisson["percall_count"], "req_per_s": round(poisson["percall_req_per_s"], 1),
+                        "gbs": round(poisson["percall_gbs"], 2), "p50_ms": round(poisson["percall_p50_s"] * 1e3, 3),
+                        "p99_ms": round(poisson["percall_p99_s"] * 1e3, 3)},
+            "saturated_vs_percall": round(ss["req_per_s"] / max(poisson["percall_req_per_s"], 1e-9), 2)}
+
+
 # ------------------------------------------------------------------ CPU arm
 def run_cpu(host_in, nthreads, min_seconds):
     """The oracle (CPU restatement of the reference path, OpenMP over the
@@ -393,6 +434,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mix", action="store_true", help="skip the batched uneven-mix measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--only", choices=["mix", "serve"], default=None,
+                    help="run only the uneven-mix or the serving measurement and print it")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch of the dominant kernel from an ncu capture")
     ap.add_argument("--specialize", type=int, default=1,
@@ -409,7 +453,7 @@ def main():
         for c in args.case:
             dt, n, b = c.split(":")
             _CASES.append((dt, int(n), int(b)))
-        args.no_e2e = args.no_cpu = args.no_mix = True
+        args.no_e2e = args.no_cpu = args.no_mix = args.no_serve = True
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     config = {"workload": "mixed-radix complex forward: nfft 480,1000,3003,65536 x float32,Q15,Q31, "
@@ -440,6 +484,11 @@ def main():
                 "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
+    if args.only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_mix(args) if args.only == "mix" else run_serving(args)))
+        return
     r = run_gpu(args)
     cpu = r["cpu"]
     if rank == 0:
@@ -448,7 +497,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
                 "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
-                "batched_mix": r["mix"],
+                "batched_mix": r["mix"], "serving": r["serving"],
                 "kernels": ("plan-specialised (NVRTC)" if args.specialize else "precompiled families") +
                 ("; autotuned" if args.autotune else "") + "; set-up before warm-up %.1f s" % r["prepare_s"]}
         print(json.dumps(line))

@@ -174,6 +174,7 @@ typedef struct {
     long long completed, failed, batches, max_batch, peak_hbm_bytes;
     double p50_s, p99_s, max_s, mean_s; /* latency, submit to completion */
     double req_per_s, gbs, bytes;       /* over first submit .. last completion */
+    double host_s;                      /* host time spent describing and launching batches */
 } kfg_serve_stats;
 typedef struct kfg_server kfg_server;
 /* hbm_budget: bytes (0 = 40 GiB); slots: batches in flight (0 = 4) */

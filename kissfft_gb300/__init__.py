@@ -331,11 +331,29 @@ def kiss_fastfir(cfg, inbuf, outbuf, n_new, offset):
     return int(n)
 
 
+def _float32_count(buf, what):
+    """Element count of a float32 numpy array or torch tensor (anything else is refused,
+    so a byte view can never be taken for samples)."""
+    if hasattr(buf, "numel"):
+        import torch
+        if buf.dtype != torch.float32:
+            raise ValueError("%s must be a float32 tensor" % what)
+        return buf.numel()
+    import numpy as np
+    if getattr(buf, "dtype", None) != np.float32:
+        raise ValueError("%s must be a float32 array" % what)
+    return buf.size
+
+
 def kiss_fastfir_filter(cfg, x, y):
     """Whole-signal fast FIR: y[:nx-ntaps+1] = valid convolution of x with the taps."""
     L = cfg.lib
+    nx = _float32_count(x, "x")
+    ny = _float32_count(y, "y")
+    ntaps = getattr(cfg, "ntaps", 1)
+    if ny < nx - ntaps + 1:
+        raise ValueError("y holds %d samples; the valid convolution has %d" % (ny, nx - ntaps + 1))
     _use_torch_stream(L, x, y)
-    nx = x.numel() if hasattr(x, "numel") else x.size
     n = L.kiss_fastfir_cuda_filter(ctypes.c_void_p(cfg.ptr), _ptr(x)[0], int(nx), _ptr(y)[0])
     _raise_on_status(L, "kiss_fastfir_filter")
     return int(n)
@@ -389,7 +407,8 @@ class ServeReq(ctypes.Structure):
 
 class ServeStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_longlong) for n in ("completed", "failed", "batches", "max_batch", "peak_hbm_bytes")] + \
-               [(n, ctypes.c_double) for n in ("p50_s", "p99_s", "max_s", "mean_s", "req_per_s", "gbs", "bytes")]
+               [(n, ctypes.c_double) for n in ("p50_s", "p99_s", "max_s", "mean_s", "req_per_s", "gbs", "bytes",
+                                               "host_s")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -22,10 +22,20 @@ inline long long launch_grid(const void* k, const Step& st) {
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
             if (nsm <= 0) nsm = 1;
         }
-        int per = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, st.cfg.T, (size_t)st.cfg.smem) != cudaSuccess ||
-            per <= 0)
-            per = 1;
+        // occupancy of the last (kernel, threads, shared memory) this thread asked for
+        thread_local const void* ck = nullptr;
+        thread_local int cT = 0, cS = 0, cper = 1;
+        if (k != ck || st.cfg.T != cT || st.cfg.smem != cS) {
+            int per = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, st.cfg.T, (size_t)st.cfg.smem) != cudaSuccess ||
+                per <= 0)
+                per = 1;
+            ck = k;
+            cT = st.cfg.T;
+            cS = st.cfg.smem;
+            cper = per;
+        }
+        const int per = cper;
         const long long cap = (long long)per * nsm;
         if (grid > cap) grid = cap;
     }

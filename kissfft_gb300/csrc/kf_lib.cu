@@ -78,6 +78,27 @@ std::unique_ptr<DevPlan> make_devplan(int dtype, int n, int inverse, int real_nf
     return dp;
 }
 
+// Pinned (page-locked, device-mapped) host memory: the kernels read and
+// write it directly over the host link.
+bool is_pinned_host_ptr(const void* ptr) {
+    if (!ptr) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer == ptr;
+}
+
+bool zero_copy_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("KISSFFT_GB300_ZEROCOPY");
+        on = (e && *e == '0') ? 0 : 1;
+    }
+    return on == 1;
+}
+
 bool is_device_ptr(const void* ptr) {
     if (!ptr) return false;
     cudaPointerAttributes a;
@@ -117,7 +138,8 @@ struct kfg_plan {
 
 namespace {
 
-int run_schedule(Schedule& s, const void* in, void* out, cudaStream_t st, const void* firH = nullptr) {
+int run_schedule(Schedule& s, const void* in, void* out, cudaStream_t st, const void* firH = nullptr,
+                 bool allow_tma = true) {
     void* scratch = nullptr;
     const size_t off1 = (s.scratch[0] + 255) & ~(size_t)255;
     const size_t tot = off1 + s.scratch[1];
@@ -128,7 +150,7 @@ int run_schedule(Schedule& s, const void* in, void* out, cudaStream_t st, const 
         step.args.in = roles[step.in_role];
         step.args.out = roles[step.out_role];
         step.args.fir_H = firH;
-        enable_tma(step, step.args.in);
+        if (allow_tma) enable_tma(step, step.args.in);
         cudaError_t e = launch_step(step, st);
         if (e != cudaSuccess) {
             rc = fail(KFG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -238,6 +260,15 @@ int exec_staged(Schedule& s, const void* in, void* out, size_t in_bytes, size_t 
                 const void* firH = nullptr) {
     const bool din = is_device_ptr(in), dout = is_device_ptr(out);
     if (din && dout) return run_schedule(s, in, out, st, firH);
+    if (zero_copy_enabled() && (din || is_pinned_host_ptr(in)) && (dout || is_pinned_host_ptr(out))) {
+        // pinned host buffers: the passes read and write them in place over
+        // the host link (no staging copies); bulk tile copies stay off
+        int rc = run_schedule(s, in, out, st, firH, false);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (rc == KFG_OK && e != cudaSuccess)
+            rc = fail(KFG_ECUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+        return rc;
+    }
     void *sin = (void*)in, *sout = out;
     if (!din) {
         KFG_CK(cudaMallocAsync(&sin, in_bytes, st));

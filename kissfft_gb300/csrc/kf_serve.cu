@@ -9,16 +9,18 @@
 //     device bytes of the admitted-but-unfinished requests (input + output +
 //     two-pass scratch) stay within the budget; a request larger than the
 //     whole budget fails at once;
-//  2. batching -- everything admitted since the last launch becomes one batch
-//     on a free slot (a stream of its own, up to KFG_SERVE_SLOTS batches in
-//     flight), so requests that arrive while others run join the next batch
-//     and overlap with them on the device;
-//  3. per batch -- one device allocation (stream-ordered, from the memory
-//     pool) holds every request's input and output, laid out by plan; pinned
-//     host inputs are gathered into it by one zero-copy kernel over the
-//     host link, other host inputs by cudaMemcpyAsync; each plan group runs
-//     as one batched launch sequence (kfg_exec_batch); fast-FIR requests run
-//     as their own block launches; outputs are scattered back the same way;
+//  2. batching -- what was admitted since the last launch (up to 1/(2*slots)
+//     of the budget) becomes one batch on a free slot (a stream of its own,
+//     up to KFG_SERVE_SLOTS batches in flight), so requests that arrive while
+//     others run join the next batch and overlap with them on the device;
+//  3. per batch (on the slot's own launcher thread) -- one device allocation (stream-ordered, from the memory
+//     pool) holds every request's input and output, laid out by plan; small
+//     pinned host inputs are gathered into it by one zero-copy kernel over
+//     the host link, large or pageable ones by the copy engines
+//     (cudaMemcpyAsync); each plan group runs
+//     as one batched launch sequence (kfg_exec_batch), fast-FIR requests as
+//     their own block launches, all forked over the slot's sub-streams so
+//     the small launches overlap; outputs are scattered back the same way;
 //  4. completion -- a host callback at the end of the batch's stream work
 //     stamps the completion time; the worker then releases the budget and
 //     wakes waiters.
@@ -64,25 +66,47 @@ struct CopyItem {
     long long bytes;
 };
 
-// One CTA per item (grid-stride over items), 16-byte words when both ends
-// and the length allow, else 4-byte words, else bytes.  Host-side pointers
-// are pinned memory the device reads or writes over the host link.
-__global__ void kf_copy_items_kernel(const CopyItem* items, int n) {
-    for (int it = blockIdx.x; it < n; it += gridDim.x) {
-        const CopyItem c = items[it];
-        const unsigned long long a = (unsigned long long)c.src | (unsigned long long)c.dst | (unsigned long long)c.bytes;
+// Item blockIdx.y, its 64 KiB chunks spread over the blockIdx.x CTAs (so a
+// large request is copied by many CTAs at once); 16-byte words when both
+// ends and the length allow, else 4-byte words, else bytes.  Host-side
+// pointers are pinned memory the device reads or writes over the host link.
+constexpr long long kChunk = 64 * 1024;
+__global__ void kf_copy_items_kernel(const CopyItem* items) {
+    const CopyItem c = items[blockIdx.y];
+    const unsigned long long a = (unsigned long long)c.src | (unsigned long long)c.dst | (unsigned long long)c.bytes;
+    for (long long lo = (long long)blockIdx.x * kChunk; lo < c.bytes; lo += (long long)gridDim.x * kChunk) {
+        const long long hi = lo + kChunk < c.bytes ? lo + kChunk : c.bytes;
         if ((a & 15) == 0) {
-            const uint4* s = (const uint4*)c.src;
-            uint4* d = (uint4*)c.dst;
-            for (long long i = threadIdx.x; i < c.bytes / 16; i += blockDim.x) d[i] = s[i];
+            // four 16-byte loads in flight per thread across the host link
+            const uint4* s = (const uint4*)(c.src + lo);
+            uint4* d = (uint4*)(c.dst + lo);
+            const long long nw = (hi - lo) / 16;
+            long long i = threadIdx.x;
+            for (; i + 3 * (long long)blockDim.x < nw; i += 4 * (long long)blockDim.x) {
+                const uint4 v0 = s[i], v1 = s[i + blockDim.x], v2 = s[i + 2 * blockDim.x], v3 = s[i + 3 * blockDim.x];
+                d[i] = v0;
+                d[i + blockDim.x] = v1;
+                d[i + 2 * blockDim.x] = v2;
+                d[i + 3 * blockDim.x] = v3;
+            }
+            for (; i < nw; i += blockDim.x) d[i] = s[i];
         } else if ((a & 3) == 0) {
-            const unsigned* s = (const unsigned*)c.src;
-            unsigned* d = (unsigned*)c.dst;
-            for (long long i = threadIdx.x; i < c.bytes / 4; i += blockDim.x) d[i] = s[i];
+            const unsigned* s = (const unsigned*)(c.src + lo);
+            unsigned* d = (unsigned*)(c.dst + lo);
+            for (long long i = threadIdx.x; i < (hi - lo) / 4; i += blockDim.x) d[i] = s[i];
         } else {
-            for (long long i = threadIdx.x; i < c.bytes; i += blockDim.x) c.dst[i] = c.src[i];
+            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) c.dst[i] = c.src[i];
         }
     }
+}
+
+cudaError_t copy_items(const CopyItem* d_items, int n, long long max_bytes, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    long long gx = (max_bytes + kChunk - 1) / kChunk;
+    if (gx > 64) gx = 64;
+    if (gx < 1) gx = 1;
+    kf_copy_items_kernel<<<dim3((unsigned)gx, (unsigned)n), 256, 0, st>>>(d_items);
+    return cudaGetLastError();
 }
 
 enum { MEM_DEVICE = 0, MEM_PINNED = 1, MEM_PAGEABLE = 2 };
@@ -118,17 +142,26 @@ struct Req {
 };
 
 constexpr int kMaxBatch = 8192;
+// buffers at least this large move by the copy engines (cudaMemcpyAsync);
+// smaller pinned ones by the gather/scatter kernel, one launch per batch
+constexpr size_t kDmaBytes = 256 * 1024;
+
+constexpr int kSub = 8;  // compute sub-streams per slot
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    cudaStream_t sub[kSub] = {};
+    cudaEvent_t fork = nullptr, join[kSub] = {};
     std::vector<Req*> reqs;
     void* dbuf = nullptr;
     CopyItem* h_items = nullptr;  // pinned: gather + scatter descriptors
     CopyItem* d_items = nullptr;
     std::atomic<int> done{0};
     double t_done = 0;
-    bool busy = false;
+    bool busy = false;       // holds a batch (launching, in flight or waiting to be reaped)
+    bool to_launch = false;  // handed to the slot's launcher thread
     size_t dev_bytes = 0;
+    std::thread launcher;
 };
 
 }  // namespace
@@ -138,7 +171,7 @@ struct kfg_server {
     int nslots = 0;
     int dev = 0;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_work, cv_done, cv_launch;
     std::deque<Req*> pending;
     std::map<long long, std::unique_ptr<Req>> reqs;  // all requests not yet collected
     long long next_id = 1;
@@ -150,6 +183,7 @@ struct kfg_server {
     std::vector<double> lat;                 // completed latencies (s)
     long long completed = 0, failed = 0, batches = 0, max_batch = 0;
     double bytes_done = 0, t_first = 0, t_last = 0;
+    double host_s = 0;  // host time spent describing and launching batches
 
     ~kfg_server();
 };
@@ -254,7 +288,7 @@ int launch_batch(kfg_server* s, Slot* sl) {
     for (auto& io : in_off) {
         ioff[io.first] = io.second;
         Req* r = io.first;
-        if (r->in_mem == MEM_PINNED) {
+        if (r->in_mem == MEM_PINNED && r->in_b < kDmaBytes) {
             sl->h_items[nin++] = CopyItem{(const unsigned char*)r->d.in, base + io.second, (long long)r->in_b};
         } else {
             e = cudaMemcpyAsync(base + io.second, r->d.in, r->in_b, cudaMemcpyDefault, sl->stream);
@@ -265,7 +299,7 @@ int launch_batch(kfg_server* s, Slot* sl) {
     for (auto& oo : out_off) {
         ooff[oo.first] = oo.second;
         Req* r = oo.first;
-        if (r->out_mem == MEM_PINNED)
+        if (r->out_mem == MEM_PINNED && r->out_b < kDmaBytes)
             sl->h_items[kMaxBatch + nout++] = CopyItem{base + oo.second, (unsigned char*)r->d.out, (long long)r->out_b};
     }
     if (nin > 0)
@@ -274,28 +308,43 @@ int launch_batch(kfg_server* s, Slot* sl) {
         e = cudaMemcpyAsync(sl->d_items + kMaxBatch, sl->h_items + kMaxBatch, sizeof(CopyItem) * nout,
                             cudaMemcpyHostToDevice, sl->stream);
     if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("serve: descriptors: ") + cudaGetErrorString(e));
-    if (nin > 0) kf_copy_items_kernel<<<std::min(nin, 4096), 256, 0, sl->stream>>>(sl->d_items, nin);
-    // compute
+    long long max_in = 0, max_out = 0;
+    for (int k = 0; k < nin; ++k) max_in = std::max(max_in, sl->h_items[k].bytes);
+    for (int k = 0; k < nout; ++k) max_out = std::max(max_out, sl->h_items[kMaxBatch + k].bytes);
+    e = copy_items(sl->d_items, nin, max_in, sl->stream);
+    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("serve: gather: ") + cudaGetErrorString(e));
+    // compute: the plan groups (and fast-FIR requests) are independent, so
+    // they fork over the slot's sub-streams and join before the scatter
+    e = cudaEventRecord(sl->fork, sl->stream);
+    for (int k = 0; k < kSub && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(sl->sub[k], sl->fork, 0);
+    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("serve: fork: ") + cudaGetErrorString(e));
+    int lane = 0;
     for (auto& g : groups) {
         Req* r0 = g.second[0];
         if (r0->d.kind == KFG_SERVE_FIR) {
             for (Req* r : g.second) {
                 size_t ny = 0;
                 int rc = kfg_fir_filter(r->plan, (const float*)(base + ioff[r]), (size_t)r->d.len,
-                                        (float*)(base + ooff[r]), &ny, sl->stream);
+                                        (float*)(base + ooff[r]), &ny, sl->sub[lane++ % kSub]);
                 if (rc) r->rc = rc;
             }
             continue;
         }
         int rc = kfg_exec_batch(r0->plan, base + ioff[r0], base + ooff[r0], (long long)g.second.size(), 0, 0,
-                                sl->stream);
+                                sl->sub[lane++ % kSub]);
         if (rc)
             for (Req* r : g.second) r->rc = rc;
     }
-    if (nout > 0) kf_copy_items_kernel<<<std::min(nout, 4096), 256, 0, sl->stream>>>(sl->d_items + kMaxBatch, nout);
+    for (int k = 0; k < kSub && e == cudaSuccess; ++k) {
+        e = cudaEventRecord(sl->join[k], sl->sub[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sl->stream, sl->join[k], 0);
+    }
+    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("serve: join: ") + cudaGetErrorString(e));
+    e = copy_items(sl->d_items + kMaxBatch, nout, max_out, sl->stream);
+    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("serve: scatter: ") + cudaGetErrorString(e));
     for (auto& oo : out_off) {
         Req* r = oo.first;
-        if (r->out_mem != MEM_PINNED) {
+        if (r->out_mem != MEM_PINNED || r->out_b >= kDmaBytes) {
             e = cudaMemcpyAsync(r->d.out, base + oo.second, r->out_b, cudaMemcpyDefault, sl->stream);
             if (e != cudaSuccess) r->rc = KFG_ECUDA;
         }
@@ -321,6 +370,38 @@ void finish_req(kfg_server* s, Req* r, double t) {
         ++s->failed;
     }
     r->state.store(2);
+}
+
+// One per slot: turns the batch the worker assigned into stream work, so the
+// host cost of launching batches is spread over the slots' threads.
+void launcher_main(kfg_server* s, Slot* sl) {
+    cudaSetDevice(s->dev);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->cv_launch.wait(lk, [&] { return sl->to_launch || s->stop; });
+        if (!sl->to_launch) break;  // stopping, nothing assigned
+        sl->to_launch = false;
+        lk.unlock();
+        const double t0 = now_s();
+        int rc = launch_batch(s, sl);
+        const double dt = now_s() - t0;
+        lk.lock();
+        s->host_s += dt;
+        if (rc) {
+            // wait for what was queued before the failure, then fail the batch
+            lk.unlock();
+            cudaStreamSynchronize(sl->stream);
+            lk.lock();
+            for (Req* r : sl->reqs) {
+                r->rc = rc;
+                finish_req(s, r, now_s());
+            }
+            sl->reqs.clear();
+            sl->busy = false;
+            s->cv_done.notify_all();
+            s->cv_work.notify_all();
+        }
+    }
 }
 
 void worker_main(kfg_server* s) {
@@ -352,10 +433,16 @@ void worker_main(kfg_server* s) {
             }
         if (free_slot && !s->pending.empty()) {
             std::vector<Req*> batch;
-            while (!s->pending.empty() && (int)batch.size() < kMaxBatch) {
+            // a batch holds at most 1/(2*slots) of the budget, so several
+            // batches pipeline (copy in / compute / copy out) across slots
+            const size_t cap = std::max<size_t>(s->budget / (2 * (size_t)s->nslots), 1);
+            size_t bbytes = 0;
+            while (!s->pending.empty() && (int)batch.size() < kMaxBatch && (batch.empty() || bbytes < cap)) {
                 Req* r = s->pending.front();
                 if (r->dev_b == 0) {
+                    const double td = now_s();
                     int rc = describe(s, r);
+                    s->host_s += now_s() - td;
                     if (rc) {
                         s->pending.pop_front();
                         r->rc = rc;
@@ -376,6 +463,7 @@ void worker_main(kfg_server* s) {
                 if (s->used + r->dev_b > s->budget) break;  // wait for memory to free up
                 s->pending.pop_front();
                 s->used += r->dev_b;
+                bbytes += r->dev_b;
                 r->state.store(1);
                 batch.push_back(r);
             }
@@ -383,23 +471,11 @@ void worker_main(kfg_server* s) {
             if (!batch.empty()) {
                 free_slot->reqs = batch;
                 free_slot->busy = true;
+                free_slot->done.store(0);
+                free_slot->to_launch = true;
                 ++s->batches;
                 s->max_batch = std::max<long long>(s->max_batch, (long long)batch.size());
-                lk.unlock();
-                int rc = launch_batch(s, free_slot);
-                lk.lock();
-                if (rc) {
-                    // nothing of this batch is in flight past the failure point's stream order;
-                    // wait for what was queued, then fail the batch
-                    cudaStreamSynchronize(free_slot->stream);
-                    for (Req* r : free_slot->reqs) {
-                        r->rc = rc;
-                        finish_req(s, r, now_s());
-                    }
-                    free_slot->reqs.clear();
-                    free_slot->busy = false;
-                    s->cv_done.notify_all();
-                }
+                s->cv_launch.notify_all();
                 continue;
             }
         }
@@ -420,7 +496,15 @@ kfg_server::~kfg_server() {
     }
     cv_work.notify_all();
     if (worker.joinable()) worker.join();
+    cv_launch.notify_all();
+    for (auto& sl : slots)
+        if (sl->launcher.joinable()) sl->launcher.join();
     for (auto& sl : slots) {
+        for (int k = 0; k < kSub; ++k) {
+            if (sl->sub[k]) cudaStreamDestroy(sl->sub[k]);
+            if (sl->join[k]) cudaEventDestroy(sl->join[k]);
+        }
+        if (sl->fork) cudaEventDestroy(sl->fork);
         if (sl->stream) cudaStreamDestroy(sl->stream);
         if (sl->h_items) cudaFreeHost(sl->h_items);
         if (sl->d_items) cudaFree(sl->d_items);
@@ -452,7 +536,15 @@ kfg_server* kfg_server_create(size_t hbm_budget, int slots) {
             if (sl->h_items) cudaFreeHost(sl->h_items);
             return nullptr;
         }
+        bool ok = cudaEventCreateWithFlags(&sl->fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int k = 0; k < kSub && ok; ++k)
+            ok = cudaStreamCreateWithFlags(&sl->sub[k], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&sl->join[k], cudaEventDisableTiming) == cudaSuccess;
         s->slots.push_back(std::move(sl));
+        if (!ok) {
+            set_error(KFG_ECUDA, "serve: sub-stream set-up failed");
+            return nullptr;
+        }
     }
     // keep freed batch buffers in the pool between batches
     cudaMemPool_t pool;
@@ -461,6 +553,7 @@ kfg_server* kfg_server_create(size_t hbm_budget, int slots) {
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
     kfg_server* raw = s.release();
+    for (auto& sl : raw->slots) sl->launcher = std::thread(launcher_main, raw, sl.get());
     raw->worker = std::thread(worker_main, raw);
     return raw;
 }
@@ -545,6 +638,7 @@ int kfg_server_stats(kfg_server* s, kfg_serve_stats* out) {
         out->gbs = s->bytes_done / span / 1e9;
     }
     out->bytes = s->bytes_done;
+    out->host_s = s->host_s;
     return KFG_OK;
 }
 
@@ -554,6 +648,7 @@ int kfg_server_reset_stats(kfg_server* s) {
     s->lat.clear();
     s->completed = s->failed = s->batches = s->max_batch = 0;
     s->bytes_done = s->t_first = s->t_last = 0;
+    s->host_s = 0;
     s->peak_used = s->used;
     return KFG_OK;
 }
