@@ -22,6 +22,8 @@ Printed JSON line (one, on rank 0):
           from a CUDA graph against the plain per-call form
   serving  the serving loop under Poisson arrivals: p50/p99 latency and
           throughput, saturated throughput, and the per-call form
+  other_configs  the 1024-point round trip, real 4096 x 65536 forward and
+          inverse, 2-D 2048^2 and real 3-D 128^3, each timed alone
 
 --impl reference times that CPU path on the same workload instead.
 """
@@ -233,6 +235,9 @@ def run_gpu(args):
     serving = None
     if not args.no_serve:
         serving = run_serving(args)
+    others = None
+    if not args.no_configs:
+        others = run_configs(args)
     cpu = None
     if not args.no_cpu:
         from oracle import kfo
@@ -242,7 +247,7 @@ def run_gpu(args):
                "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs)}
     return {"value": value, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e, "clocks": clocks, "cpu": cpu,
             "gpu_launches": args.steps * sum(launches_per_unit), "alg_bytes": alg_bytes,
-            "prepare_s": round(t_prep, 2), "mix": mix, "serving": serving}
+            "prepare_s": round(t_prep, 2), "mix": mix, "serving": serving, "others": others}
 
 
 # ------------------------------------------------------------------ uneven mix
@@ -366,6 +371,149 @@ def run_mix(args, count=MIX_COUNT):
             "max_rel_diff_vs_percall": worst, "commit_and_tune_s": round(t_commit, 2)}
 
 
+def run_mix_runs(args):
+    """Profiling form of the uneven mix: one kfg_batch of the 20,000 requests
+    (256 threads per tile), run --steps times back to back (no per-call form)."""
+    import ctypes
+
+    import torch
+
+    import inputs
+    import kissfft_gb300 as kf
+
+    L = kf.core()
+    vp, ll, ci = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int
+    L.kfg_batch_create.restype = vp
+    L.kfg_batch_add.argtypes = [vp, ci, ci, ci, ll, ll]
+    L.kfg_batch_commit.argtypes = [vp, vp, vp, ci]
+    L.kfg_batch_run.argtypes = [vp, vp]
+    L.kfg_batch_free.argtypes = [vp]
+    kf.set_specialize(False)
+    kinds, dts = {"c2c": 1, "r2c": 2}, {"float": 0, "int16_t": 2}
+    B = L.kfg_batch_create()
+    io = oo = 0
+    for kind, d, n in inputs.uneven_mix(MIX_COUNT, seed=3):
+        ib = n * ESZ[d] if kind == "c2c" else n * 4
+        ob = n * ESZ[d] if kind == "c2c" else (n // 2 + 1) * 8
+        L.kfg_batch_add(B, kinds[kind], dts[d], n, io, oo)
+        io = (io + ib + 255) // 256 * 256
+        oo = (oo + ob + 255) // 256 * 256
+    ind = torch.zeros(io, dtype=torch.uint8, device="cuda")
+    outd = torch.zeros(oo, dtype=torch.uint8, device="cuda")
+    if L.kfg_batch_commit(B, vp(ind.data_ptr()), vp(outd.data_ptr()), 256) != 0:
+        raise RuntimeError(L.kfg_last_error().decode())
+    st = vp(torch.cuda.current_stream().cuda_stream)
+    times = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        L.kfg_batch_run(B, st)
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t) * 1e3)
+    L.kfg_batch_free(B)
+    return {"runs_ms": [round(x, 3) for x in times]}
+
+
+def run_serve_burst(args):
+    """Profiling form of the serving loop: 3,000 requests of the serving mix
+    submitted at once (seed 5), 40 GB budget, 4 slots."""
+    import kissfft_gb300 as kf
+
+    kf.set_specialize(False)
+    srv = kf.Server(hbm_budget=40 << 30, slots=4)
+    try:
+        r = srv.loadtest(rate=0.0, count=3000, seed=5, percall_max=0)
+    finally:
+        srv.close()
+    return r
+
+
+# ------------------------------------------------------------------ other configs
+def run_configs(args):
+    """The reference's other workloads, each timed alone (back-to-back
+    launches between two events, after a warm launch): the 1024-point
+    forward+inverse round trip on 4096 transforms (seed 0); kiss_fftr and
+    kiss_fftri at nfft 4096 on 65536 rows of 3 unit sinusoids + N(0, 0.1^2)
+    noise (generated on the device, seed 2); kiss_fftnd on a 2048x2048
+    complex array; kiss_fftndr / kiss_fftndri on a 128^3 real array.  GB/s of
+    compulsory bytes (c2c 2*N*8, r2c 4N + 8(N/2+1), nd 2*prod*8, ndr
+    4*prod + 8*prod/N*(N/2+1) per transform)."""
+    import torch
+
+    import inputs
+    import kissfft_gb300 as kf
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    peak, _ = peaks()
+    reps = max(3, args.steps // 2)
+    kf.set_specialize(args.specialize)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def row(byts, ms, note):
+        return {"ms": round(ms, 4), "gbs": round(byts / ms / 1e6, 1), "frac_of_measured_peak": round(byts / ms / 1e6 / peak, 3),
+                "note": note}
+
+    out = {}
+    # config 1: complex 1024 forward then inverse, 4096 transforms
+    x = torch.from_numpy(inputs.cpx((4096, 1024), "float", 0).view(np.float32).copy()).to(dev)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    fw, iv = kf.kiss_fft_alloc(1024, 0), kf.kiss_fft_alloc(1024, 1)
+    for c in (fw, iv):
+        kf.autotune(c, 4096)
+        kf.prepare(c, 4096)
+    ms = timed(lambda: (kf.kiss_fft_batch(fw, x, y, 4096), kf.kiss_fft_batch(iv, y, z, 4096)))
+    out["c2c_1024_fwd_inv_4096"] = row(2 * 2 * 1024 * 8 * 4096, ms, "32 MiB each way: L2-resident")
+    del x, y, z
+    # config 3: real 4096 x 65536 (1 GiB of reals)
+    B, N = 65536, 4096
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    t = torch.arange(N, device=dev, dtype=torch.float32)
+    tr = torch.empty((B, N), device=dev, dtype=torch.float32)
+    for r0 in range(0, B, 8192):
+        f = torch.rand((8192, 3, 1), device=dev, generator=g) * (N / 2)
+        ph = torch.rand((8192, 3, 1), device=dev, generator=g) * 6.283185307179586
+        tr[r0:r0 + 8192] = torch.cos(6.283185307179586 * f * t / N + ph).sum(1) + \
+            0.1 * torch.randn((8192, N), device=dev, generator=g)
+    fr = torch.empty((B, N // 2 + 1, 2), device=dev, dtype=torch.float32)
+    back = torch.empty_like(tr)
+    rf, ri = kf.kiss_fftr_alloc(N, 0), kf.kiss_fftr_alloc(N, 1)
+    for c in (rf, ri):
+        kf.autotune(c, B)
+        kf.prepare(c, B)
+    rbytes = (4 * N + 8 * (N // 2 + 1)) * B
+    out["r2c_4096_65536"] = row(rbytes, timed(lambda: kf.kiss_fftr_batch(rf, tr, fr, B)), "1 GiB in")
+    out["c2r_4096_65536"] = row(rbytes, timed(lambda: kf.kiss_fftri_batch(ri, fr, back, B)), "1 GiB out")
+    del tr, fr, back
+    # config 3: 2-D complex 2048^2 and real 128^3
+    a = torch.from_numpy(inputs.cpx((2048, 2048), "float", 2).view(np.float32).copy()).to(dev)
+    b = torch.empty_like(a)
+    nd = kf.kiss_fftnd_alloc([2048, 2048], 0)
+    out["nd_2048x2048"] = row(2 * 2048 * 2048 * 8, timed(lambda: kf.kiss_fftnd(nd, a, b)), "32 MiB: L2-resident")
+    rng = np.random.default_rng(2)
+    v = torch.from_numpy(rng.standard_normal((128, 128, 128)).astype(np.float32)).to(dev)
+    w = torch.empty((128, 128, 65, 2), device=dev, dtype=torch.float32)
+    v2 = torch.empty_like(v)
+    ndr, ndri = kf.kiss_fftndr_alloc([128, 128, 128], 0), kf.kiss_fftndr_alloc([128, 128, 128], 1)
+    nbytes = 4 * 128 ** 3 + 8 * 128 * 128 * 65
+    out["ndr_128^3"] = row(nbytes, timed(lambda: kf.kiss_fftndr(ndr, v, w)), "8 MiB: L2-resident")
+    out["ndri_128^3"] = row(nbytes, timed(lambda: kf.kiss_fftndri(ndri, w, v2)), "8 MiB: L2-resident")
+    return out
+
+
 # ------------------------------------------------------------------ serving loop
 def run_serving(args):
     """Serving loop (kfg_server, 40 GB HBM budget): Poisson arrivals at
@@ -435,7 +583,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mix", action="store_true", help="skip the batched uneven-mix measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--only", choices=["mix", "serve"], default=None,
+    ap.add_argument("--no-configs", action="store_true", help="skip the real / N-D / round-trip workloads")
+    ap.add_argument("--only", choices=["mix", "serve", "configs", "mix-runs", "serve-burst"], default=None,
                     help="run only the uneven-mix or the serving measurement and print it")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch of the dominant kernel from an ncu capture")
@@ -453,7 +602,7 @@ def main():
         for c in args.case:
             dt, n, b = c.split(":")
             _CASES.append((dt, int(n), int(b)))
-        args.no_e2e = args.no_cpu = args.no_mix = args.no_serve = True
+        args.no_e2e = args.no_cpu = args.no_mix = args.no_serve = args.no_configs = True
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     config = {"workload": "mixed-radix complex forward: nfft 480,1000,3003,65536 x float32,Q15,Q31, "
@@ -487,7 +636,9 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(0)
-        print(json.dumps(run_mix(args) if args.only == "mix" else run_serving(args)))
+        fn = {"mix": run_mix, "serve": run_serving, "configs": run_configs, "mix-runs": run_mix_runs,
+              "serve-burst": run_serve_burst}[args.only]
+        print(json.dumps(fn(args)))
         return
     r = run_gpu(args)
     cpu = r["cpu"]
@@ -497,7 +648,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
                 "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
-                "batched_mix": r["mix"], "serving": r["serving"],
+                "batched_mix": r["mix"], "serving": r["serving"], "other_configs": r["others"],
                 "kernels": ("plan-specialised (NVRTC)" if args.specialize else "precompiled families") +
                 ("; autotuned" if args.autotune else "") + "; set-up before warm-up %.1f s" % r["prepare_s"]}
         print(json.dumps(line))
