@@ -46,6 +46,10 @@ SIZES = [480, 1000, 3003, 65536]
 DTYPES = ["float", "int16_t", "int32_t"]
 ESZ = {"float": 8, "double": 16, "int16_t": 4, "int32_t": 8}
 BATCH_BYTES = 256 * 1024 * 1024
+# DRAM bytes (read + write) per launch measured by ncu on these exact
+# launches (profiles/ncu_engine_kernels_bench_sizes.md); the write figure
+# misses the dirty lines still in L2 when the capture ends
+NCU_TRAFFIC = {("int32_t", 3003, 11173): 496.2e6, ("float", 1000, 33554): 485.8e6}
 
 
 def peaks():
@@ -206,7 +210,9 @@ def run_gpu(args):
     roof = {"bound": "hbm", "kernel": "kf_engine_kernel %s nfft=%d batch=%d (%d launch%s)" % (
         dt_, n_, b_, launches_per_unit[dom], "es" if launches_per_unit[dom] > 1 else ""),
         "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
-        "frac": round(achieved / peak, 4), "traffic": args.traffic}
+        "frac": round(achieved / peak, 4),
+        "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC.get((dt_, n_, b_)),
+        "traffic_unit": "DRAM bytes per launch (ncu)", "algorithmic_bytes": dom_bytes}
     # e2e: host pinned buffers through the C ABI (H2D + D2H inside the timed region)
     e2e = None
     if not args.no_e2e:
