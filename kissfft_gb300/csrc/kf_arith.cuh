@@ -76,29 +76,61 @@ struct ArFixed {
     static KF_HD W neg(W a) { return (W)(0u - (uint32_t)a); }
     static KF_HD W half(W a) { return a >> 1; }
     static KF_HD S sround(P x) { return (S)((x + ((P)1 << (FB - 1))) >> FB); }
-    static KF_HD S smul(S a, S b) { return sround((P)a * (P)b); }
+    // sround(a*b + c*d) as an untruncated word (exact: |a*b + c*d| < 2^(2*FB+1))
+    static KF_HD W round2(S a, S b, S c, S d) {
+#if defined(__CUDA_ARCH__)
+        if constexpr (sizeof(P) == 8) {
+            // Q31: two signed 32x32+64 multiply-adds, then bits 31..62 of the
+            // 64-bit sum (the low word of the arithmetic shift)
+            long long t;
+            unsigned lo, hi, r;
+            asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"((int)a), "r"((int)b), "l"(1ll << (FB - 1)));
+            asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"((int)c), "r"((int)d), "l"(t));
+            asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(t));
+            asm("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(lo), "r"(hi), "r"(FB));
+            return (W)r;
+        }
+#endif
+        return (W)(((P)a * (P)b + (P)c * (P)d + ((P)1 << (FB - 1))) >> FB);
+    }
+    // sround(a*b) as an untruncated word
+    static KF_HD W round1(S a, S b) {
+#if defined(__CUDA_ARCH__)
+        if constexpr (sizeof(P) == 8) {
+            long long t;
+            unsigned lo, hi, r;
+            asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"((int)a), "r"((int)b), "l"(1ll << (FB - 1)));
+            asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(t));
+            asm("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(lo), "r"(hi), "r"(FB));
+            return (W)r;
+        }
+#endif
+        return (W)(((P)a * (P)b + ((P)1 << (FB - 1))) >> FB);
+    }
+    static KF_HD S smul(S a, S b) { return (S)round1(a, b); }
+    // C_MUL(m, a, b) with b a table twiddle (|b| <= SMAX, so -b.i fits S)
     static KF_HD C cmul(C a, C b) {
         C m;
-        m.r = sround((P)a.r * (P)b.r - (P)a.i * (P)b.i);
-        m.i = sround((P)a.r * (P)b.i + (P)a.i * (P)b.r);
+        m.r = (S)round2(a.r, b.r, a.i, (S)(0 - b.i));
+        m.i = (S)round2(a.r, b.i, a.i, b.r);
         return m;
     }
     template <int Q>
     static KF_HD C fixdiv(C c) {
-        const P k = (P)(SMAX / Q);
-        c.r = sround((P)c.r * k);
-        c.i = sround((P)c.i * k);
+        constexpr S k = (S)(SMAX / Q);
+        c.r = (S)round1(c.r, k);
+        c.i = (S)round1(c.i, k);
         return c;
     }
     static KF_HD C fixdiv_rt(C c, int q) {
-        const P k = (P)(SMAX / q);
-        c.r = sround((P)c.r * k);
-        c.i = sround((P)c.i * k);
+        const S k = (S)(SMAX / q);
+        c.r = (S)round1(c.r, k);
+        c.i = (S)round1(c.i, k);
         return c;
     }
     static KF_HD C mulsc(C c, S s) {
-        c.r = sround((P)c.r * (P)s);
-        c.i = sround((P)c.i * (P)s);
+        c.r = (S)round1(c.r, s);
+        c.i = (S)round1(c.i, s);
         return c;
     }
     // C_MUL(t, a, w) then C_ADDTO(acc, t) of kf_bfly_generic, with acc kept as
@@ -107,12 +139,8 @@ struct ArFixed {
     // |w| <= SMAX, so -w.i fits S and every product is one widening
     // multiply-add; the sums are exact in P (|a*w| < 2^(2*FB)).
     static KF_HD void cmul_acc(W& ar, W& ai, C a, C w) {
-        const P rnd = (P)1 << (FB - 1);
-        const S nwi = (S)(0 - w.i);
-        const P re = (P)a.r * (P)w.r + (P)a.i * (P)nwi + rnd;
-        const P im = (P)a.r * (P)w.i + (P)a.i * (P)w.r + rnd;
-        ar = add(ar, (W)(re >> FB));
-        ai = add(ai, (W)(im >> FB));
+        ar = add(ar, round2(a.r, w.r, a.i, (S)(0 - w.i)));
+        ai = add(ai, round2(a.r, w.i, a.i, w.r));
     }
 };
 

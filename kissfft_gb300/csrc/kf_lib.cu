@@ -331,7 +331,7 @@ std::string plan_sig(const kfg_plan* p) {
         snprintf(name, sizeof(name), "%s", prop.name);
     for (char* c = name; *c; ++c)
         if (*c == ' ') *c = '_';
-    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v2";
+    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v3";
     return o.str();
 }
 
@@ -679,7 +679,13 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
                 Step c = base;
                 if (J < 1 || (J != base.cfg.J && !reshape_step(c, J))) continue;
                 const int m0 = c.cfg.minb;
-                for (int mb : {1, m0, m0 + 1}) {
+                // register budgets: none, the default, a little and a lot
+                // tighter, and the occupancy that threads and shared memory allow
+                const int maxb = std::max(1, std::min(std::min(2048 / std::max(c.cfg.T, 32),
+                                                               (227 * 1024) / std::max(c.cfg.smem + 1024, 1)),
+                                                      32));
+                for (int mb : {1, m0, m0 + 1, m0 + 2, 2 * m0, maxb}) {
+                    if (mb < 1 || mb > maxb) continue;
                     bool dup = false;
                     for (auto& d : cands)
                         dup |= (d.cfg.J == c.cfg.J && d.cfg.minb == mb && d.args.col_in == c.args.col_in);
