@@ -152,7 +152,8 @@ void kfg_batch_free(kfg_batch *b);
  * continuously (everything admitted since the last launch goes out together,
  * up to KFG_SERVE_SLOTS batches in flight on their own streams), and
  * completed asynchronously.  Plans and fast-FIR responses stay cached on the
- * device.  Buffers may be device, pinned host (moved by one zero-copy
+ * device; their bytes count against the budget and the least recently used
+ * plan no request holds is evicted when the budget runs out.  Buffers may be device, pinned host (moved by one zero-copy
  * gather/scatter kernel per batch) or ordinary host memory, and must stay
  * valid until the request is waited for.  Latency = completion - submit. */
 #define KFG_SERVE_C2C 1    /* kiss_fft:   n0 points, dtype, inverse        */
@@ -175,6 +176,7 @@ typedef struct {
     double p50_s, p99_s, max_s, mean_s; /* latency, submit to completion */
     double req_per_s, gbs, bytes;       /* over first submit .. last completion */
     double host_s;                      /* host time spent describing and launching batches */
+    long long plans, plan_bytes, evictions; /* device plan cache: entries, bytes, LRU evictions */
 } kfg_serve_stats;
 typedef struct kfg_server kfg_server;
 /* hbm_budget: bytes (0 = 40 GiB); slots: batches in flight (0 = 4) */

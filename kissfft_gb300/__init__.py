@@ -408,7 +408,8 @@ class ServeReq(ctypes.Structure):
 class ServeStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_longlong) for n in ("completed", "failed", "batches", "max_batch", "peak_hbm_bytes")] + \
                [(n, ctypes.c_double) for n in ("p50_s", "p99_s", "max_s", "mean_s", "req_per_s", "gbs", "bytes",
-                                               "host_s")]
+                                               "host_s")] + \
+               [(n, ctypes.c_longlong) for n in ("plans", "plan_bytes", "evictions")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -1144,6 +1144,17 @@ __attribute__((visibility("hidden"))) int c2c_schedule(kfg_plan* p, long long ba
     return build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
 }
 __attribute__((visibility("hidden"))) int set_error(int code, const std::string& msg) { return fail(code, msg); }
+// device bytes a plan holds (tables of every sub-plan, fast-FIR response)
+__attribute__((visibility("hidden"))) size_t plan_device_bytes(const kfg_plan* p) {
+    if (!p) return 0;
+    size_t b = 0;
+    if (p->main) b += p->main->p.blob.size();
+    if (p->aux) b += p->aux->p.blob.size();
+    for (auto& a : p->axes)
+        if (a) b += a->p.blob.size();
+    if (p->d_H) b += (size_t)(p->n / 2 + 1) * 8;
+    return b;
+}
 __attribute__((visibility("hidden"))) bool device_pointer(const void* ptr) { return is_device_ptr(ptr); }
 __attribute__((visibility("hidden"))) cudaStream_t stream_or_default(void* stream) { return pick(stream); }
 }  // namespace kf

@@ -26,7 +26,9 @@
 //     wakes waiters.
 //
 // Plans (and fast-FIR filter responses, keyed by the taps' contents) stay
-// cached on the device for the server's lifetime.  Latency = completion
+// cached on the device; their bytes count against the budget, and the least
+// recently used plan that no pending or admitted request holds is evicted
+// when plans + requests would pass it.  Latency = completion
 // stamp - submit stamp (steady clock), so p50/p99 include queueing.
 #include <string.h>
 
@@ -47,7 +49,9 @@
 
 namespace kf {
 int set_error(int code, const std::string& msg);
+size_t plan_device_bytes(const kfg_plan* p);
 }
+using kf::plan_device_bytes;
 using kf::set_error;
 
 namespace {
@@ -179,7 +183,19 @@ struct kfg_server {
     bool stop = false;
     std::thread worker;
     std::vector<std::unique_ptr<Slot>> slots;
-    std::map<std::string, kfg_plan*> plans;  // nd and fast-FIR plans owned here
+    // device plan cache: every plan the loop uses, least recently used
+    // evicted first once plans + admitted requests would pass the budget;
+    // a plan pinned by a pending or admitted request is never evicted
+    struct PlanEntry {
+        kfg_plan* plan = nullptr;
+        size_t bytes = 0;
+        unsigned long long last = 0;
+        int pins = 0;
+    };
+    std::map<std::string, PlanEntry> plans;
+    size_t plan_bytes = 0;
+    unsigned long long tick = 0;
+    long long evictions = 0;
     std::vector<double> lat;                 // completed latencies (s)
     long long completed = 0, failed = 0, batches = 0, max_batch = 0;
     double bytes_done = 0, t_first = 0, t_last = 0;
@@ -190,17 +206,68 @@ struct kfg_server {
 
 namespace {
 
-// device bytes, plan key and plan of a request (called on the worker)
+// Evict unpinned plans, least recently used first, until plans + admitted
+// requests + `extra` fit the budget (or nothing is left to evict).
+void evict_lru(kfg_server* s, size_t extra) {
+    while (s->used + s->plan_bytes + extra > s->budget) {
+        auto victim = s->plans.end();
+        for (auto it = s->plans.begin(); it != s->plans.end(); ++it)
+            if (it->second.pins == 0 && (victim == s->plans.end() || it->second.last < victim->second.last))
+                victim = it;
+        if (victim == s->plans.end()) return;
+        s->plan_bytes -= victim->second.bytes;
+        kfg_plan_free(victim->second.plan);
+        s->plans.erase(victim);
+        ++s->evictions;
+    }
+}
+
+// The cached plan of `key` (built by make() on a miss), pinned for one request.
+kfg_plan* pin_plan(kfg_server* s, const std::string& key, kfg_plan* (*make)(const kfg_serve_req&),
+                   const kfg_serve_req& d) {
+    auto it = s->plans.find(key);
+    if (it == s->plans.end()) {
+        kfg_plan* p = make(d);
+        if (!p) return nullptr;
+        kfg_server::PlanEntry e;
+        e.plan = p;
+        e.bytes = plan_device_bytes(p);
+        s->plan_bytes += e.bytes;
+        it = s->plans.emplace(key, e).first;
+        it->second.pins = 1;  // not a victim of its own admission
+        evict_lru(s, 0);
+        it->second.pins = 0;
+    }
+    it->second.pins++;
+    it->second.last = ++s->tick;
+    return it->second.plan;
+}
+
+void unpin_plan(kfg_server* s, const std::string& key) {
+    auto it = s->plans.find(key);
+    if (it != s->plans.end() && it->second.pins > 0) it->second.pins--;
+}
+
+kfg_plan* make_c2c(const kfg_serve_req& d) { return kfg_plan_c2c(d.dtype, d.n0, d.inverse ? 1 : 0); }
+kfg_plan* make_real(const kfg_serve_req& d) { return kfg_plan_real(d.dtype, d.n0, d.kind == KFG_SERVE_C2R); }
+kfg_plan* make_2d(const kfg_serve_req& d) {
+    const int dims[2] = {d.n0, d.n1};
+    return kfg_plan_nd(d.dtype, dims, 2, d.inverse ? 1 : 0);
+}
+kfg_plan* make_fir(const kfg_serve_req& d) { return kfg_plan_fir(d.taps, (size_t)d.n0, 0, nullptr); }
+
+// device bytes, plan key and (pinned) plan of a request (called on the worker)
 int describe(kfg_server* s, Req* r) {
     const kfg_serve_req& d = r->d;
     const int esz = cpx_bytes_of(d.dtype), rsz = esz / 2;
     char key[160];
+    kfg_plan* (*make)(const kfg_serve_req&) = nullptr;
     switch (d.kind) {
         case KFG_SERVE_C2C:
             if (d.n0 < 1) return set_error(KFG_EINVAL, "serve: bad length");
             r->in_b = r->out_b = (size_t)d.n0 * esz;
-            r->plan = kfg_plan_cached(0, d.dtype, d.n0, d.inverse);
             snprintf(key, sizeof(key), "c:%d:%d:%d", d.dtype, d.n0, d.inverse ? 1 : 0);
+            make = make_c2c;
             break;
         case KFG_SERVE_R2C:
         case KFG_SERVE_C2R: {
@@ -208,42 +275,28 @@ int describe(kfg_server* s, Req* r) {
             const size_t nb = (size_t)(d.n0 / 2 + 1) * esz, nr = (size_t)d.n0 * rsz;
             r->in_b = d.kind == KFG_SERVE_R2C ? nr : nb;
             r->out_b = d.kind == KFG_SERVE_R2C ? nb : nr;
-            r->plan = kfg_plan_cached(1, d.dtype, d.n0, d.kind == KFG_SERVE_C2R);
             snprintf(key, sizeof(key), "r:%d:%d:%d", d.dtype, d.n0, d.kind == KFG_SERVE_C2R);
+            make = make_real;
             break;
         }
-        case KFG_SERVE_C2C_2D: {
+        case KFG_SERVE_C2C_2D:
             if (d.n0 < 1 || d.n1 < 1) return set_error(KFG_EINVAL, "serve: bad 2-D shape");
             r->in_b = r->out_b = (size_t)d.n0 * d.n1 * esz;
             snprintf(key, sizeof(key), "n:%d:%dx%d:%d", d.dtype, d.n0, d.n1, d.inverse ? 1 : 0);
-            auto it = s->plans.find(key);
-            if (it == s->plans.end()) {
-                const int dims[2] = {d.n0, d.n1};
-                kfg_plan* p = kfg_plan_nd(d.dtype, dims, 2, d.inverse);
-                if (!p) return KFG_EINVAL;
-                it = s->plans.emplace(key, p).first;
-            }
-            r->plan = it->second;
+            make = make_2d;
             break;
-        }
-        case KFG_SERVE_FIR: {
+        case KFG_SERVE_FIR:
             if (d.dtype != KFG_FLOAT || !d.taps || d.n0 < 1 || d.len < d.n0)
                 return set_error(KFG_EINVAL, "serve: fast FIR needs float taps and a signal at least as long");
             r->in_b = (size_t)d.len * 4;
             r->out_b = (size_t)(d.len - d.n0 + 1) * 4;
             snprintf(key, sizeof(key), "f:%d:%016llx", d.n0, fnv1a(d.taps, (size_t)d.n0 * 4));
-            auto it = s->plans.find(key);
-            if (it == s->plans.end()) {
-                kfg_plan* p = kfg_plan_fir(d.taps, (size_t)d.n0, 0, nullptr);
-                if (!p) return KFG_EINVAL;
-                it = s->plans.emplace(key, p).first;
-            }
-            r->plan = it->second;
+            make = make_fir;
             break;
-        }
         default:
             return set_error(KFG_EINVAL, "serve: unknown request kind");
     }
+    r->plan = pin_plan(s, key, make, d);
     if (!r->plan) return KFG_EINVAL;
     r->key = key;
     // two-pass plans allocate scratch of one more copy of the data
@@ -360,6 +413,7 @@ int launch_batch(kfg_server* s, Slot* sl) {
 void finish_req(kfg_server* s, Req* r, double t) {
     r->t_done = t;
     s->used -= r->dev_b;
+    unpin_plan(s, r->key);
     if (r->rc == 0) {
         ++s->completed;
         s->lat.push_back(t - r->t_submit);
@@ -451,7 +505,10 @@ void worker_main(kfg_server* s) {
                         s->cv_done.notify_all();
                         continue;
                     }
-                    if (r->dev_b > s->budget) {
+                    const auto pe = s->plans.find(r->key);
+                    const size_t own = pe != s->plans.end() ? pe->second.bytes : 0;
+                    if (r->dev_b + own > s->budget) {
+                        unpin_plan(s, r->key);
                         s->pending.pop_front();
                         r->rc = set_error(KFG_ENOMEM, "serve: request larger than the HBM budget");
                         r->state.store(2);
@@ -460,7 +517,8 @@ void worker_main(kfg_server* s) {
                         continue;
                     }
                 }
-                if (s->used + r->dev_b > s->budget) break;  // wait for memory to free up
+                if (s->used + s->plan_bytes + r->dev_b > s->budget) evict_lru(s, r->dev_b);
+                if (s->used + s->plan_bytes + r->dev_b > s->budget) break;  // wait for memory to free up
                 s->pending.pop_front();
                 s->used += r->dev_b;
                 bbytes += r->dev_b;
@@ -509,7 +567,7 @@ kfg_server::~kfg_server() {
         if (sl->h_items) cudaFreeHost(sl->h_items);
         if (sl->d_items) cudaFree(sl->d_items);
     }
-    for (auto& kv : plans) kfg_plan_free(kv.second);
+    for (auto& kv : plans) kfg_plan_free(kv.second.plan);
 }
 
 extern "C" {
@@ -639,6 +697,9 @@ int kfg_server_stats(kfg_server* s, kfg_serve_stats* out) {
     }
     out->bytes = s->bytes_done;
     out->host_s = s->host_s;
+    out->plans = (long long)s->plans.size();
+    out->plan_bytes = (long long)s->plan_bytes;
+    out->evictions = s->evictions;
     return KFG_OK;
 }
 

@@ -196,6 +196,35 @@ def test_admission_under_a_small_budget(kf):
         srv.close()
 
 
+def test_plan_cache_evicts_under_the_budget(kf):
+    """Ten plan sizes cycled through a 2 MiB budget: plans (about 0.4 MiB
+    each) are evicted least recently used first, never while a request holds
+    them, and every result stays right."""
+    sizes = [16384, 15625, 16200, 15552, 16000, 15360, 14580, 14400, 13824, 13500]
+    srv = kf.Server(hbm_budget=2 << 20, slots=2)
+    try:
+        xs, ys, ids = [], [], []
+        for k in range(30):
+            n = sizes[k % len(sizes)]
+            x = inputs.cpx((n,), "float", 900 + k)
+            y = np.zeros_like(x)
+            xs.append(x)
+            ys.append(y)
+            ids.append(srv.submit(kf.SERVE_C2C, x, y, n))
+        for rid in ids:
+            assert srv.wait(rid, timeout=60.0) is not None
+        for k in (0, 13, 29):
+            n = sizes[k % len(sizes)]
+            assert close("c2c", "float", n, ys[k], alone(kf, "c2c", "float", n, xs[k]))
+        st = srv.stats()
+        assert st["completed"] == 30 and st["failed"] == 0
+        assert st["evictions"] > 0
+        assert st["peak_hbm_bytes"] <= 2 << 20
+        assert st["plan_bytes"] <= 2 << 20
+    finally:
+        srv.close()
+
+
 def test_loadtest_runs(kf):
     """A short Poisson load (2,000 req/s for 0.5 s) completes every request."""
     srv = kf.Server()
