@@ -6,6 +6,7 @@ produces, under kissfft_gb300/lib/:
     libkissfft_gb300.so          core: plans, schedules, sm_103a kernels
     libkissfft_cuda-<type>.so    drop-in C ABI (include/kiss_fft_cuda.h) for
                                  type in float, double, int16_t, int32_t
+    fftutil_cuda-<type>          the tools/fftutil.c stream front end on the GPU
 
 The kernels are compiled once per (sample type, kernel family) pair from
 csrc/kf_inst.cu, all translation units in parallel, for sm_103a only.
@@ -69,6 +70,11 @@ def core_lib():
 
 def dropin_lib(dtype):
     return os.path.join(LIB, "libkissfft_cuda-%s.so" % dtype)
+
+
+def fftutil_bin(dtype):
+    """The raw-binary stream tool of one sample type (csrc/kf_fftutil.c)."""
+    return os.path.join(LIB, "fftutil_cuda-%s" % dtype)
 
 
 def _digest(paths, flags):
@@ -147,6 +153,12 @@ def build(verbose=False, jobs=None):
                                                       "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart",
                                                       "-Wl,-rpath,$ORIGIN"]
         _compile(cmd, [os.path.join(CSRC, "kf_dropin.cpp"), core] + hdrs, out, verbose)
+    for i, dt in enumerate(DTYPES):
+        out = fftutil_bin(dt)
+        cmd = ["gcc", "-O2", "-Wall", "-DKF_TOOL_DTYPE=%d" % i, "-I", INC, "-I", os.path.join(CUDA_HOME, "include"),
+               os.path.join(CSRC, "kf_fftutil.c"), "-o", out, "-L", LIB, "-lkissfft_gb300",
+               "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN"]
+        _compile(cmd, [os.path.join(CSRC, "kf_fftutil.c"), core] + hdrs, out, verbose)
     return LIB
 
 

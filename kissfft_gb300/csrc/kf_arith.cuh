@@ -70,10 +70,24 @@ template <typename S, typename P, int FB, int64_t SMAX>
 struct ArFixed {
     typedef int32_t W;
     typedef cpx<S> C;
+    // truncation to the storage width (mod 2^16 for Q15)
     static KF_HD S st(W x) { return (S)x; }
     static KF_HD W add(W a, W b) { return (W)((uint32_t)a + (uint32_t)b); }
     static KF_HD W sub(W a, W b) { return (W)((uint32_t)a - (uint32_t)b); }
-    static KF_HD W neg(W a) { return (W)(0u - (uint32_t)a); }
+    // Negation as a 32-bit word.  For Q15 it is opaque on the device: when
+    // the optimizer could see a 16-bit sample being negated and then
+    // truncated, it compiled -(-32768) as if it fitted 16 bits (32768
+    // instead of the reference's wrap to -32768).
+    static KF_HD W neg(W a) {
+#if defined(__CUDA_ARCH__)
+        if constexpr (sizeof(S) == 2) {
+            int r;
+            asm("sub.s32 %0, 0, %1;" : "=r"(r) : "r"((int)a));
+            return (W)r;
+        }
+#endif
+        return (W)(0u - (uint32_t)a);
+    }
     static KF_HD W half(W a) { return a >> 1; }
     static KF_HD S sround(P x) { return (S)((x + ((P)1 << (FB - 1))) >> FB); }
     // sround(a*b + c*d) as an untruncated word (exact: |a*b + c*d| < 2^(2*FB+1))
@@ -107,30 +121,30 @@ struct ArFixed {
 #endif
         return (W)(((P)a * (P)b + ((P)1 << (FB - 1))) >> FB);
     }
-    static KF_HD S smul(S a, S b) { return (S)round1(a, b); }
+    static KF_HD S smul(S a, S b) { return st(round1(a, b)); }
     // C_MUL(m, a, b) with b a table twiddle (|b| <= SMAX, so -b.i fits S)
     static KF_HD C cmul(C a, C b) {
         C m;
-        m.r = (S)round2(a.r, b.r, a.i, (S)(0 - b.i));
-        m.i = (S)round2(a.r, b.i, a.i, b.r);
+        m.r = st(round2(a.r, b.r, a.i, (S)(0 - b.i)));
+        m.i = st(round2(a.r, b.i, a.i, b.r));
         return m;
     }
     template <int Q>
     static KF_HD C fixdiv(C c) {
         constexpr S k = (S)(SMAX / Q);
-        c.r = (S)round1(c.r, k);
-        c.i = (S)round1(c.i, k);
+        c.r = st(round1(c.r, k));
+        c.i = st(round1(c.i, k));
         return c;
     }
     static KF_HD C fixdiv_rt(C c, int q) {
         const S k = (S)(SMAX / q);
-        c.r = (S)round1(c.r, k);
-        c.i = (S)round1(c.i, k);
+        c.r = st(round1(c.r, k));
+        c.i = st(round1(c.i, k));
         return c;
     }
     static KF_HD C mulsc(C c, S s) {
-        c.r = (S)round1(c.r, s);
-        c.i = (S)round1(c.i, s);
+        c.r = st(round1(c.r, s));
+        c.i = st(round1(c.i, s));
         return c;
     }
     // C_MUL(t, a, w) then C_ADDTO(acc, t) of kf_bfly_generic, with acc kept as

@@ -298,3 +298,51 @@ def test_error_behaviour(kf):
         kf.kiss_fftri(fw, f, t)                         # improper alloc, kiss_fftr.c:124-127
     assert kf.kiss_fft_alloc(0, 0) is None
     assert kf.kiss_fftndr_alloc([4, 5], 0) is None       # odd real axis
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t"])
+def test_fixed_point_most_negative_samples(kf, dtype):
+    """Inputs with the most negative sample (-32768 / -2^31) at 5% of the
+    positions: negations and sums that wrap must truncate exactly as the
+    reference's stores do (a device compile once turned -(-32768) into
+    32768).  c2c over radices 2..5 and generic, real forward and inverse,
+    and N-D, all bit for bit against the oracle."""
+    import torch
+    rng = np.random.default_rng(11)
+    lo = np.iinfo(np.int16 if dtype == "int16_t" else np.int32).min
+
+    def spiked(a):
+        a = a.copy()
+        a[rng.random(a.shape) < 0.05] = lo
+        return a
+
+    for n in (480, 1000, 3003, 4096, 65536):
+        b = 8
+        x = spiked(inputs.cpx((b, n), dtype, n + 3))
+        for inv in (0, 1):
+            cfg = kf.kiss_fft_alloc(n, inv, dtype)
+            yd = empty_dev(x)
+            kf.kiss_fft_batch(cfg, to_dev(x), yd, b)
+            assert sha(from_dev(yd, x)) == sha(kfo.fft(x, inv, dtype)), (n, inv)
+            cfg.free()
+    for nfft in (1024, 6006):
+        b = 16
+        t = spiked(inputs.real((b, nfft), dtype, nfft))
+        f = spiked(inputs.cpx((b, nfft // 2 + 1), dtype, nfft + 1))
+        fw = kf.kiss_fftr_alloc(nfft, 0, dtype)
+        iv = kf.kiss_fftr_alloc(nfft, 1, dtype)
+        fd = empty_dev(kfo.empty_cpx((b, nfft // 2 + 1), dtype))
+        kf.kiss_fftr_batch(fw, to_dev(t), fd, b)
+        assert sha(from_dev(fd, kfo.empty_cpx((b, nfft // 2 + 1), dtype))) == sha(kfo.fftr(t, dtype)), nfft
+        td = torch.zeros((b, nfft), dtype=getattr(torch, kfo.SCALAR[dtype].__name__), device="cuda")
+        kf.kiss_fftri_batch(iv, to_dev(f), td, b)
+        torch.cuda.synchronize()
+        assert sha(td.cpu().numpy()) == sha(kfo.fftri(f, nfft, dtype)), nfft
+        fw.free()
+        iv.free()
+    x = spiked(inputs.cpx((24, 40), dtype, 9))
+    cfg = kf.kiss_fftnd_alloc([24, 40], 0, dtype)
+    yd = empty_dev(x)
+    kf.kiss_fftnd(cfg, to_dev(x), yd)
+    assert sha(from_dev(yd, x)) == sha(kfo.fftnd(x, [24, 40], 0, dtype))
+    cfg.free()
