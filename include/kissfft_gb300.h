@@ -88,6 +88,11 @@ int kfg_exec_batch_noalloc(kfg_plan *p, const void *in, void *out, long long bat
  * convolution); *ny_out gets that count. */
 int kfg_fir_filter(kfg_plan *p, const float *x, size_t nx, float *y, size_t *ny_out, void *stream);
 
+/* The packing step of the C++ facade's transform_real (kissfft.hh:154-189):
+ * bins[0..n] of a 2n-point real transform (device, float or double) ->
+ * dst[0] = (X0, Xn), dst[k] = X[k] (conj != 0: conj(X[k])), k = 1..n-1. */
+int kfg_pack_real(int dtype, const void *bins, void *dst, long long n, int conj, void *stream);
+
 int kfg_set_stream(void *stream);
 void *kfg_get_stream(void);
 int kfg_synchronize(void);

@@ -112,6 +112,22 @@ bool is_device_ptr(const void* ptr) {
 
 cudaStream_t pick(void* stream) { return stream ? (cudaStream_t)stream : g_stream.load(); }
 
+// kissfft.hh transform_real packing (kissfft.hh:154-189): bins X[0..n] of a
+// 2n-point real transform -> dst[0] = (X0, Xn), dst[k] = X[k] (conjugated
+// for the facade's inverse flag), k = 1..n-1.  One thread per output.
+template <typename T>
+__global__ void kf_pack_real_kernel(const T* X, T* dst, long long n, int conj) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (k == 0) {
+        dst[0] = X[0];
+        dst[1] = X[2 * n];
+    } else {
+        dst[2 * k] = X[2 * k];
+        dst[2 * k + 1] = conj ? -X[2 * k + 1] : X[2 * k + 1];
+    }
+}
+
 // scale the fast FIR response by the reference's float(1.0/nfft)
 __global__ void kf_scale_kernel(float* H, long long n, float s) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -580,6 +596,20 @@ int kfg_fir_filter(kfg_plan* p, const float* x, size_t nx, float* y, size_t* ny_
     Schedule s;
     if (!schedule_fastfir(p->main->p, p->aux->p, p->ntaps, (long long)nx, 0, s)) return fail(KFG_EINVAL, s.error);
     return exec_staged(s, x, y, nx * sizeof(float), (size_t)nout * sizeof(float), pick(stream), p->d_H);
+}
+
+int kfg_pack_real(int dtype, const void* bins, void* dst, long long n, int conj, void* stream) {
+    if ((dtype != KFG_FLOAT && dtype != KFG_DOUBLE) || !bins || !dst || n < 1)
+        return fail(KFG_EINVAL, "kfg_pack_real: float or double bins and n >= 1");
+    if (!is_device_ptr(bins) || !is_device_ptr(dst)) return fail(KFG_EINVAL, "kfg_pack_real: device pointers only");
+    const cudaStream_t st = pick(stream);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (dtype == KFG_FLOAT)
+        kf_pack_real_kernel<float><<<grid, 256, 0, st>>>((const float*)bins, (float*)dst, n, conj);
+    else
+        kf_pack_real_kernel<double><<<grid, 256, 0, st>>>((const double*)bins, (double*)dst, n, conj);
+    KFG_CK(cudaGetLastError());
+    return KFG_OK;
 }
 
 int kfg_set_stream(void* stream) {
