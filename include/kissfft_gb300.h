@@ -93,6 +93,17 @@ int kfg_fir_filter(kfg_plan *p, const float *x, size_t nx, float *y, size_t *ny_
  * dst[0] = (X0, Xn), dst[k] = X[k] (conj != 0: conj(X[k])), k = 1..n-1. */
 int kfg_pack_real(int dtype, const void *bins, void *dst, long long n, int conj, void *stream);
 
+/* Power spectrogram of tools/psdpng.c (transform_signal, psdpng.c:116-175;
+ * the PNG output is not part of this library): 16-bit samples (stereo != 0:
+ * interleaved pairs, summed), frames of nfft with their mean removed when
+ * remove_dc != 0, a real forward FFT per frame, and per row of navg frames
+ * rows[r][k] = 10*log10(sum |X[k]|^2 / navg + 1), k = 0..nfft/2.  p: a float
+ * forward real plan of nfft.  nsamples counts samples per channel; only
+ * whole rows are produced (*nrows_out gets their number).  Buffers may be
+ * host or device memory. */
+int kfg_psd(kfg_plan *p, const short *samples, long long nsamples, int stereo, int remove_dc, int navg, float *rows,
+            long long *nrows_out, void *stream);
+
 int kfg_set_stream(void *stream);
 void *kfg_get_stream(void);
 int kfg_synchronize(void);

@@ -523,3 +523,32 @@ class Server(object):
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- tools/psdpng.c
+def psd(samples, nfft, navg, stereo=False, remove_dc=False):
+    """Power spectrogram of psdpng (tools/psdpng.c:116-175): 16-bit samples
+    (interleaved pairs summed when stereo), frames of nfft (mean removed when
+    remove_dc), rows of navg frames, 10*log10(mean |X|^2 + 1) per frequency.
+    Returns a (rows, nfft/2+1) float32 array."""
+    import numpy as np
+    L = core()
+    L.kfg_psd.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                          ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.c_void_p]
+    x = np.ascontiguousarray(samples, dtype=np.int16)
+    per_channel = x.size // 2 if stereo else x.size
+    nrows = per_channel // nfft // navg
+    rows = np.zeros((nrows, nfft // 2 + 1), np.float32)
+    plan = L.kfg_plan_real(DTYPE_CODE["float"], int(nfft), 0)
+    if not plan:
+        raise KissFFTError("kfg_plan_real: " + L.kfg_last_error().decode())
+    try:
+        got = ctypes.c_longlong(0)
+        rc = L.kfg_psd(ctypes.c_void_p(plan), x.ctypes.data, per_channel, int(bool(stereo)), int(bool(remove_dc)),
+                       int(navg), rows.ctypes.data if nrows else None, ctypes.byref(got), None)
+        if rc:
+            raise KissFFTError("kfg_psd: " + L.kfg_last_error().decode())
+        assert got.value == nrows
+    finally:
+        L.kfg_plan_free(ctypes.c_void_p(plan))
+    return rows

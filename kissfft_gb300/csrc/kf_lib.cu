@@ -128,6 +128,49 @@ __global__ void kf_pack_real_kernel(const T* X, T* dst, long long n, int conj) {
     }
 }
 
+// psdpng's frame preparation (tools/psdpng.c:134-155): 16-bit samples
+// (stereo: the two channels summed) to float, optionally minus the frame's
+// mean.  One CTA per frame.
+__global__ void kf_psd_prep_kernel(const short* in, float* t, int nfft, int stereo, int remove_dc) {
+    __shared__ float part[32];
+    const long long f = blockIdx.x;
+    float* tf = t + f * nfft;
+    float sum = 0.f;
+    for (int i = threadIdx.x; i < nfft; i += blockDim.x) {
+        const long long j = f * nfft + i;
+        const float v = stereo ? (float)(in[2 * j] + in[2 * j + 1]) : (float)in[j];
+        tf[i] = v;
+        sum += v;
+    }
+    if (!remove_dc) return;
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float s = threadIdx.x < (blockDim.x + 31) / 32 ? part[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) part[0] = s;
+    }
+    __syncthreads();
+    const float avg = part[0] / nfft;
+    for (int i = threadIdx.x; i < nfft; i += blockDim.x) tf[i] -= avg;
+}
+
+// psdpng's row (tools/psdpng.c:160-170): 10*log10(sum over navg frames of
+// |X|^2 / navg + 1) per frequency.  One thread per (row, frequency).
+__global__ void kf_psd_reduce_kernel(const float* bins, float* rows, long long nrows, int nfreqs, int navg) {
+    const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nrows * nfreqs) return;
+    const long long r = it / nfreqs;
+    const int k = (int)(it - r * nfreqs);
+    float m = 0.f;
+    for (int a = 0; a < navg; ++a) {
+        const float* b = bins + 2 * ((r * navg + a) * nfreqs + k);
+        m += b[0] * b[0] + b[1] * b[1];
+    }
+    rows[it] = 10.f * log10f(m / navg + 1.f);
+}
+
 // scale the fast FIR response by the reference's float(1.0/nfft)
 __global__ void kf_scale_kernel(float* H, long long n, float s) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -610,6 +653,56 @@ int kfg_pack_real(int dtype, const void* bins, void* dst, long long n, int conj,
         kf_pack_real_kernel<double><<<grid, 256, 0, st>>>((const double*)bins, (double*)dst, n, conj);
     KFG_CK(cudaGetLastError());
     return KFG_OK;
+}
+
+int kfg_psd(kfg_plan* p, const short* samples, long long nsamples, int stereo, int remove_dc, int navg, float* rows,
+            long long* nrows_out, void* stream) {
+    if (!p || p->kind != K_REAL || p->inverse || p->dtype != KFG_FLOAT || !samples || !rows || navg < 1 || nsamples < 0)
+        return fail(KFG_EINVAL, "kfg_psd: a forward float real plan, samples, rows and navg >= 1");
+    const long long nfft = p->n, nfreqs = nfft / 2 + 1;
+    const long long nrows = nsamples / nfft / navg, nframes = nrows * navg;  // whole rows only
+    if (nrows_out) *nrows_out = nrows;
+    if (nrows == 0) return KFG_OK;
+    const cudaStream_t st = pick(stream);
+    const bool din = is_device_ptr(samples), dout = is_device_ptr(rows);
+    const size_t in_bytes = (size_t)nframes * nfft * (stereo ? 2 : 1) * sizeof(short);
+    const size_t t_bytes = (size_t)nframes * nfft * sizeof(float), b_bytes = (size_t)nframes * nfreqs * 8;
+    const size_t r_bytes = (size_t)nrows * nfreqs * sizeof(float);
+    void *d_in = (void*)samples, *d_t = nullptr, *d_b = nullptr, *d_rows = rows;
+    KFG_CK(cudaMallocAsync(&d_t, t_bytes, st));
+    KFG_CK(cudaMallocAsync(&d_b, b_bytes, st));
+    if (!din) {
+        KFG_CK(cudaMallocAsync(&d_in, in_bytes, st));
+        KFG_CK(cudaMemcpyAsync(d_in, samples, in_bytes, cudaMemcpyHostToDevice, st));
+    }
+    if (!dout) KFG_CK(cudaMallocAsync(&d_rows, r_bytes, st));
+    kf_psd_prep_kernel<<<(unsigned)nframes, 256, 0, st>>>((const short*)d_in, (float*)d_t, (int)nfft, stereo ? 1 : 0,
+                                                          remove_dc ? 1 : 0);
+    int rc = KFG_OK;
+    if (cudaGetLastError() != cudaSuccess) rc = fail(KFG_ECUDA, "kfg_psd: frame kernel");
+    Schedule s;
+    size_t ib = 0, ob = 0;
+    if (rc == KFG_OK) rc = build_schedule(p, nframes, 0, 1, 0, s, ib, ob);
+    if (rc == KFG_OK) rc = run_schedule(s, d_t, d_b, st);
+    if (rc == KFG_OK) {
+        const long long items = nrows * nfreqs;
+        kf_psd_reduce_kernel<<<(unsigned)((items + 255) / 256), 256, 0, st>>>((const float*)d_b, (float*)d_rows, nrows,
+                                                                              (int)nfreqs, navg);
+        if (cudaGetLastError() != cudaSuccess) rc = fail(KFG_ECUDA, "kfg_psd: row kernel");
+    }
+    if (rc == KFG_OK && !dout) {
+        cudaError_t e = cudaMemcpyAsync(rows, d_rows, r_bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) rc = fail(KFG_ECUDA, std::string("kfg_psd: D2H: ") + cudaGetErrorString(e));
+    }
+    cudaFreeAsync(d_t, st);
+    cudaFreeAsync(d_b, st);
+    if (!din) cudaFreeAsync(d_in, st);
+    if (!dout) cudaFreeAsync(d_rows, st);
+    if (!din || !dout) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (rc == KFG_OK && e != cudaSuccess) rc = fail(KFG_ECUDA, std::string("kfg_psd: ") + cudaGetErrorString(e));
+    }
+    return rc;
 }
 
 int kfg_set_stream(void* stream) {
