@@ -90,6 +90,17 @@ bool is_pinned_host_ptr(const void* ptr) {
     return a.type == cudaMemoryTypeHost && a.devicePointer == ptr;
 }
 
+// large host batches: chunked copy/compute/copy pipeline (default on;
+// KISSFFT_GB300_PIPELINE=0 keeps the zero-copy kernels for every size)
+bool pipeline_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("KISSFFT_GB300_PIPELINE");
+        on = (e && *e == '0') ? 0 : 1;
+    }
+    return on == 1;
+}
+
 bool zero_copy_enabled() {
     static int on = -1;
     if (on < 0) {
@@ -605,6 +616,127 @@ kfg_plan* kfg_plan_fir(const float* taps, size_t ntaps, size_t nfft, size_t* nff
 
 void kfg_plan_free(kfg_plan* p) { delete p; }
 
+}  // extern "C"
+
+namespace {
+
+// Streams, events and a ring of device buffers for pipelined host calls,
+// one set per host thread.
+struct HostPipe {
+    static constexpr int kSlots = 3;
+    cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+    cudaEvent_t start = nullptr, ev_in[kSlots] = {}, ev_comp[kSlots] = {}, ev_out[kSlots] = {};
+    unsigned char *din = nullptr, *dout = nullptr;  // ring, kept between calls
+    size_t din_cap = 0, dout_cap = 0;
+    bool ok = false;
+    bool reserve(size_t in_bytes, size_t out_bytes) {
+        if (in_bytes > din_cap) {
+            if (din) cudaFree(din);
+            din = nullptr;
+            din_cap = 0;
+            if (cudaMalloc((void**)&din, in_bytes) != cudaSuccess) return false;
+            din_cap = in_bytes;
+        }
+        if (out_bytes > dout_cap) {
+            if (dout) cudaFree(dout);
+            dout = nullptr;
+            dout_cap = 0;
+            if (cudaMalloc((void**)&dout, out_bytes) != cudaSuccess) return false;
+            dout_cap = out_bytes;
+        }
+        return true;
+    }
+    HostPipe() {
+        ok = cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&comp, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&start, cudaEventDisableTiming) == cudaSuccess;
+        for (int k = 0; k < kSlots && ok; ++k)
+            ok = cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&ev_comp[k], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&ev_out[k], cudaEventDisableTiming) == cudaSuccess;
+    }
+};
+
+// A large packed 1-D batch on page-locked host buffers, in chunks of about
+// 32 MiB: chunk i+1's copy in, chunk i's kernels and chunk i-1's copy out
+// run at the same time on three streams (both directions of the host link
+// busy at once), through a ring of three device buffers per side kept per
+// host thread.  Returns 1 when the call does not qualify (the caller takes
+// another path).
+int exec_pipelined(kfg_plan* p, const void* in, void* out, long long batch, long long in_dist, long long out_dist,
+                   cudaStream_t caller) {
+    if (p->kind != K_C2C && p->kind != K_REAL) return 1;
+    const long long n = p->n, nb = n / 2 + 1;
+    const int esz = esz_of(p->dtype), rsz = esz / 2;
+    long long in_frame, out_frame;  // bytes of one transform
+    if (p->kind == K_C2C)
+        in_frame = out_frame = n * esz;
+    else if (!p->inverse)
+        in_frame = n * rsz, out_frame = nb * esz;
+    else
+        in_frame = nb * esz, out_frame = n * rsz;
+    const long long in_elem = p->kind == K_C2C || p->inverse ? esz : rsz;
+    const long long out_elem = p->kind == K_C2C || !p->inverse ? esz : rsz;
+    if ((in_dist && in_dist * in_elem != in_frame) || (out_dist && out_dist * out_elem != out_frame)) return 1;
+    const long long cb = std::max(1LL, (32LL << 20) / std::max(in_frame, out_frame));
+    const long long nch = (batch + cb - 1) / cb;
+    if (nch < 4) return 1;
+    thread_local HostPipe pipe;
+    if (!pipe.ok) return 1;
+    const int S = HostPipe::kSlots;
+    // the previous call on this thread has finished (it synchronised), so
+    // the ring may be regrown here
+    if (!pipe.reserve((size_t)(S * cb * in_frame), (size_t)(S * cb * out_frame)))
+        return fail(KFG_ENOMEM, "pipelined host call: device ring");
+    unsigned char *din = pipe.din, *dout = pipe.dout;
+    KFG_CK(cudaEventRecord(pipe.start, caller));
+    KFG_CK(cudaStreamWaitEvent(pipe.h2d, pipe.start, 0));
+    KFG_CK(cudaStreamWaitEvent(pipe.comp, pipe.start, 0));
+    KFG_CK(cudaStreamWaitEvent(pipe.d2h, pipe.start, 0));
+    int rc = KFG_OK;
+    for (long long i = 0; i < nch && rc == KFG_OK; ++i) {
+        const int k = (int)(i % S);
+        const long long b0 = i * cb, nbt = std::min(cb, batch - b0);
+        unsigned char* di = din + (size_t)k * cb * in_frame;
+        unsigned char* dq = dout + (size_t)k * cb * out_frame;
+        Schedule s;
+        size_t ib = 0, ob = 0;
+        rc = build_schedule(p, nbt, 0, 1, 0, s, ib, ob);
+        if (rc) break;
+        cudaError_t e = cudaSuccess;
+        if (i >= S) e = cudaStreamWaitEvent(pipe.h2d, pipe.ev_comp[k], 0);  // slot's input consumed
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(di, (const unsigned char*)in + b0 * in_frame, (size_t)(nbt * in_frame),
+                                cudaMemcpyHostToDevice, pipe.h2d);
+        if (e == cudaSuccess) e = cudaEventRecord(pipe.ev_in[k], pipe.h2d);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(pipe.comp, pipe.ev_in[k], 0);
+        if (e == cudaSuccess && i >= S) e = cudaStreamWaitEvent(pipe.comp, pipe.ev_out[k], 0);  // output copied out
+        if (e != cudaSuccess) {
+            rc = fail(KFG_ECUDA, std::string("pipelined copy in: ") + cudaGetErrorString(e));
+            break;
+        }
+        rc = run_schedule(s, di, dq, pipe.comp);
+        if (rc) break;
+        e = cudaEventRecord(pipe.ev_comp[k], pipe.comp);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(pipe.d2h, pipe.ev_comp[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync((unsigned char*)out + b0 * out_frame, dq, (size_t)(nbt * out_frame),
+                                cudaMemcpyDeviceToHost, pipe.d2h);
+        if (e == cudaSuccess) e = cudaEventRecord(pipe.ev_out[k], pipe.d2h);
+        if (e != cudaSuccess) rc = fail(KFG_ECUDA, std::string("pipelined copy out: ") + cudaGetErrorString(e));
+    }
+    cudaError_t e1 = cudaStreamSynchronize(pipe.h2d), e2 = cudaStreamSynchronize(pipe.d2h),
+                e3 = cudaStreamSynchronize(pipe.comp);
+    if (rc == KFG_OK && (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess))
+        rc = fail(KFG_ECUDA, "pipelined host call failed");
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
 int kfg_exec_batch(kfg_plan* p, const void* in, void* out, long long batch, long long in_dist, long long out_dist,
                    void* stream) {
     if (!p || !in || !out || batch < 0) return fail(KFG_EINVAL, "kfg_exec_batch: bad arguments");
@@ -615,6 +747,15 @@ int kfg_exec_batch(kfg_plan* p, const void* in, void* out, long long batch, long
     int rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
     if (rc) return rc;
     apply_tuned(p, tune_key(batch, in_dist, out_dist), s);
+    // pinned host buffers: kernels that read whole rows in one pass use
+    // them in place (zero-copy); schedules of several steps or column tiles
+    // (short runs per row over the host link) take the copy pipeline
+    bool multi = s.steps.size() > 1;
+    for (auto& st : s.steps) multi |= st.args.col_in || st.args.col_out;
+    if (multi && pipeline_enabled() && is_pinned_host_ptr(in) && is_pinned_host_ptr(out) && (const void*)out != in) {
+        rc = exec_pipelined(p, in, out, batch, in_dist, out_dist, pick(stream));
+        if (rc != 1) return rc;
+    }
     return exec_staged(s, in, out, ib, ob, pick(stream));
 }
 

@@ -99,3 +99,39 @@ def test_nd_and_fir(kf):
     assert kf.kiss_fastfir_filter(ff, sd, od) == ny
     assert np.array_equal(op.numpy(), host(od))
     ff.free()
+
+
+@pytest.mark.parametrize("dt,n,b", [("float", 4096, 5000), ("int16_t", 1000, 50000), ("float", 65536, 300)])
+def test_large_batches_pipelined(kf, dt, n, b):
+    """Batches of 128 MiB and more on pinned buffers run as a chunked
+    copy-in / kernels / copy-out pipeline: same bits as device buffers."""
+    import torch
+    x = inputs.cpx((b, n), dt, n + b)
+    cfg = kf.kiss_fft_alloc(n, 0, dt)
+    xp, yp = pinned(x), torch.zeros(x.nbytes, dtype=torch.uint8).pin_memory()
+    xd, yd = device(x), torch.zeros(x.nbytes, dtype=torch.uint8, device="cuda")
+    kf.kiss_fft_batch(cfg, xp, yp, b)
+    kf.kiss_fft_batch(cfg, xd, yd, b)
+    assert np.array_equal(yp.numpy(), host(yd))
+    cfg.free()
+
+
+def test_large_real_batches_pipelined(kf):
+    import torch
+    nfft, b = 4096, 10000
+    t = inputs.real((b, nfft), "float", 8)
+    fw = kf.kiss_fftr_alloc(nfft, 0, "float")
+    iv = kf.kiss_fftr_alloc(nfft, 1, "float")
+    nb = nfft // 2 + 1
+    fp = torch.zeros(b * nb * 8, dtype=torch.uint8).pin_memory()
+    fd = torch.zeros(b * nb * 8, dtype=torch.uint8, device="cuda")
+    kf.kiss_fftr_batch(fw, pinned(t), fp, b)
+    kf.kiss_fftr_batch(fw, device(t), fd, b)
+    assert np.array_equal(fp.numpy(), host(fd))
+    rp = torch.zeros(t.nbytes, dtype=torch.uint8).pin_memory()
+    rd = torch.zeros(t.nbytes, dtype=torch.uint8, device="cuda")
+    kf.kiss_fftri_batch(iv, fp, rp, b)
+    kf.kiss_fftri_batch(iv, fd, rd, b)
+    assert np.array_equal(rp.numpy(), host(rd))
+    fw.free()
+    iv.free()
