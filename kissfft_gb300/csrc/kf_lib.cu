@@ -200,7 +200,7 @@ struct kfg_plan {
     void* d_H = nullptr;
     // autotuned launch shapes per (batch, in_dist, out_dist): J, minb, tma per step
     std::mutex tune_mu;
-    std::map<std::string, std::vector<std::array<int, 4>>> tuned;
+    std::map<std::string, std::vector<std::array<int, 5>>> tuned;
     ~kfg_plan() {
         if (d_H) cudaFree(d_H);
     }
@@ -370,7 +370,7 @@ std::string tune_key(long long batch, long long in_dist, long long out_dist) {
     return o.str();
 }
 
-void apply_cfgs(Schedule& s, const std::vector<std::array<int, 4>>& v) {
+void apply_cfgs(Schedule& s, const std::vector<std::array<int, 5>>& v) {
     size_t k = 0;
     for (auto& st : s.steps) {
         if (st.kind != 0) continue;
@@ -378,6 +378,7 @@ void apply_cfgs(Schedule& s, const std::vector<std::array<int, 4>>& v) {
         const auto& c = v[k++];
         if (c[3] && !st.args.col_in) recolumn_step(st);
         if (c[0] != st.cfg.J) reshape_step(st, c[0]);
+        if (c[4] && c[4] != st.cfg.T) retarget_threads(st, c[4]);
         st.cfg.minb = c[1];
         st.tma_ok = c[2];
     }
@@ -401,7 +402,7 @@ std::string plan_sig(const kfg_plan* p) {
         snprintf(name, sizeof(name), "%s", prop.name);
     for (char* c = name; *c; ++c)
         if (*c == ' ') *c = '_';
-    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v3";
+    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v4";
     return o.str();
 }
 
@@ -417,7 +418,7 @@ std::string tune_file() {
     return d + "/tune.txt";
 }
 
-bool tune_load(const std::string& key, std::vector<std::array<int, 4>>& v) {
+bool tune_load(const std::string& key, std::vector<std::array<int, 5>>& v) {
     std::ifstream f(tune_file());
     std::string line;
     bool found = false;
@@ -425,16 +426,16 @@ bool tune_load(const std::string& key, std::vector<std::array<int, 4>>& v) {
         size_t sp = line.find(' ');
         if (sp == std::string::npos || line.compare(0, sp, key) != 0 || sp != key.size()) continue;
         std::istringstream is(line.substr(sp + 1));
-        std::vector<std::array<int, 4>> r;
-        std::array<int, 4> c;
-        while (is >> c[0] >> c[1] >> c[2] >> c[3]) r.push_back(c);
+        std::vector<std::array<int, 5>> r;
+        std::array<int, 5> c;
+        while (is >> c[0] >> c[1] >> c[2] >> c[3] >> c[4]) r.push_back(c);
         v = r;
         found = true;  // the last line for a key wins
     }
     return found;
 }
 
-void tune_store(const std::string& key, const std::vector<std::array<int, 4>>& v) {
+void tune_store(const std::string& key, const std::vector<std::array<int, 5>>& v) {
     std::string path = tune_file();
     std::string dir = path.substr(0, path.rfind('/'));
     std::string cmd;
@@ -442,7 +443,7 @@ void tune_store(const std::string& key, const std::vector<std::array<int, 4>>& v
         if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
     std::ofstream f(path, std::ios::app);
     f << key;
-    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2] << " " << c[3];
+    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2] << " " << c[3] << " " << c[4];
     f << "\n";
 }
 
@@ -904,7 +905,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
     if (!p || batch < 1 || p->kind == K_FIR) return fail(KFG_EINVAL, "kfg_autotune: bad arguments");
     const std::string key = tune_key(batch, in_dist, out_dist);
     const std::string dkey = plan_sig(p) + ":" + key;
-    std::vector<std::array<int, 4>> best;
+    std::vector<std::array<int, 5>> best;
     if (tune_load(dkey, best)) {
         std::lock_guard<std::mutex> lk(p->tune_mu);
         p->tuned[key] = best;
@@ -952,11 +953,28 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
                     if (mb < 1 || mb > maxb) continue;
                     bool dup = false;
                     for (auto& d : cands)
-                        dup |= (d.cfg.J == c.cfg.J && d.cfg.minb == mb && d.args.col_in == c.args.col_in);
+                        dup |= (d.cfg.J == c.cfg.J && d.cfg.T == c.cfg.T && d.cfg.minb == mb &&
+                                d.args.col_in == c.args.col_in);
                     if (dup) continue;
                     Step cm = c;
                     cm.cfg.minb = mb;
                     cands.push_back(cm);
+                }
+                // thread counts that fit one pass's groups in one or two
+                // rounds (passes with uneven group counts leave threads idle)
+                const KSub& sb = c.args.sub[0];
+                for (int pi = 0; pi < sb.npass; ++pi) {
+                    const long long G = (long long)c.cfg.J * sb.ps[pi].H * sb.ps[pi].ML;
+                    for (int r = 1; r <= 2; ++r) {
+                        const int T = (int)(((G + r - 1) / r + 31) / 32 * 32);
+                        Step ct = c;
+                        if (T == c.cfg.T || !retarget_threads(ct, T)) continue;
+                        bool dup = false;
+                        for (auto& d : cands)
+                            dup |= (d.cfg.J == ct.cfg.J && d.cfg.T == ct.cfg.T && d.cfg.minb == ct.cfg.minb &&
+                                    d.args.col_in == ct.args.col_in);
+                        if (!dup) cands.push_back(ct);
+                    }
                 }
             }
         }
@@ -971,7 +989,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
             for (auto& t : th) t.join();
         }
         float bt = -1.f;
-        std::array<int, 4> bc = {st0.cfg.J, st0.cfg.minb, 1, st0.args.col_in};
+        std::array<int, 5> bc = {st0.cfg.J, st0.cfg.minb, 1, st0.args.col_in, st0.cfg.T};
         for (auto& c : cands) {
             for (int tma = 1; tma >= 0; --tma) {
                 Step x = c;
@@ -979,7 +997,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
                 float ms = time_step(x, roles, strm, e0, e1, 3);
                 if (ms > 0 && (bt < 0 || ms < bt)) {
                     bt = ms;
-                    bc = {c.cfg.J, c.cfg.minb, tma, c.args.col_in};
+                    bc = {c.cfg.J, c.cfg.minb, tma, c.args.col_in, c.cfg.T};
                 }
                 if (!x.args.tma) break;  // staging not eligible: one timing is enough
             }
@@ -987,7 +1005,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
         best.push_back(bc);
         // later steps read what this one wrote: run it once with the winner
         Step w = st0;
-        std::vector<std::array<int, 4>> one = {bc};
+        std::vector<std::array<int, 5>> one = {bc};
         Schedule tmp;
         tmp.steps.push_back(w);
         apply_cfgs(tmp, one);

@@ -323,6 +323,16 @@ static int default_minb(int T, int smem) {
 
 static void finish(Step& st, const LaunchCfg& c);
 
+// Another thread count for an engine step (same tile): a multiple of 32 at
+// least the step's minimum, so a pass's groups fill whole rounds.
+bool retarget_threads(Step& st, int T) {
+    if (st.kind != 0 || T < 32 || T > KF_MAXT || (T & 31)) return false;
+    if (T < cfg_min_threads(st.args.sub[0], st.mode, st.cfg.J)) return false;
+    st.cfg.T = T;
+    st.cfg.minb = default_minb(T, st.cfg.smem);
+    return true;
+}
+
 bool reshape_step(Step& st, int J) {
     if (st.kind != 0 || J < 1 || J > KF_MAXJ || (J & (J - 1))) return false;
     const KSub& sb = st.args.sub[0];

@@ -79,6 +79,7 @@ int sub_family(const KSub& sb);
 struct Step;
 bool enable_tma(Step& st, const void* in);
 bool recolumn_step(Step& st);
+bool retarget_threads(Step& st, int T);
 void set_tma_enabled(int on);
 bool tma_enabled();
 
