@@ -1,0 +1,61 @@
+"""The seeded synthetic workloads (tests/golden/inputs.py) keep the shapes
+and shares their descriptions state, and every size they draw builds a plan
+(checked with the library's own plan builder through the CPU emulator)."""
+import ctypes
+import os
+
+import numpy as np
+
+import inputs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def prime_factors(n):
+    out, p = set(), 2
+    while p * p <= n:
+        while n % p == 0:
+            out.add(p)
+            n //= p
+        p += 1
+    if n > 1:
+        out.add(n)
+    return out
+
+
+def test_uneven_mix_shares_and_sizes():
+    mix = inputs.uneven_mix(4000, seed=3)
+    assert mix == inputs.uneven_mix(4000, seed=3)  # seeded
+    kinds = [(k, d) for k, d, _ in mix]
+    share = lambda kd: kinds.count(kd) / len(kinds)
+    assert abs(share(("c2c", "float")) - 0.6) < 0.03
+    assert abs(share(("r2c", "float")) - 0.3) < 0.03
+    assert abs(share(("c2c", "int16_t")) - 0.1) < 0.02
+    smooth = 0
+    for k, d, n in mix:
+        assert 16 <= n <= 131072
+        if k == "r2c":
+            assert n % 2 == 0
+        f = prime_factors(n)
+        assert max(f) <= 31
+        smooth += f <= {2, 3, 5}
+    assert abs(smooth / len(mix) - 0.8) < 0.03
+    ns = np.array([n for _, _, n in mix])
+    # log-uniform on [16, 131072]: about half the draws below the geometric mean
+    assert abs(np.mean(ns < np.sqrt(16 * 131072)) - 0.5) < 0.05
+
+
+def test_uneven_mix_sizes_build_plans():
+    lib = os.path.join(ROOT, "tests", "emu", "_build", "libkfemu.so")
+    if not os.path.exists(lib):
+        import subprocess
+        csrc = os.path.join(ROOT, "kissfft_gb300", "csrc")
+        os.makedirs(os.path.dirname(lib), exist_ok=True)
+        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wno-unknown-pragmas", "-shared", "-fPIC",
+                        "-I", csrc, os.path.join(ROOT, "tests", "emu", "kf_emu.cpp"), os.path.join(csrc, "kf_plan.cpp"),
+                        "-o", lib], check=True)
+    E = ctypes.CDLL(lib)
+    out = (ctypes.c_int * 4)()
+    for k, d, n in set(inputs.uneven_mix(20000, seed=3)):
+        dt = 0 if d == "float" else 2
+        assert E.emu_plan_info(dt, n // 2 if k == "r2c" else n, 0, out) == 0, (k, d, n)
