@@ -130,6 +130,33 @@ def _ptr(buf):
     raise TypeError("unsupported buffer type %r" % type(buf))
 
 
+_CPX_BYTES = {"float": 8, "double": 16, "int16_t": 4, "int32_t": 8}
+
+
+def _nbytes(buf):
+    """Byte size of a numpy array or torch tensor (None for a raw address)."""
+    if buf is None or isinstance(buf, int):
+        return None
+    if hasattr(buf, "element_size") and hasattr(buf, "numel"):
+        return int(buf.element_size() * buf.numel())
+    if hasattr(buf, "nbytes"):
+        return int(buf.nbytes)
+    return None
+
+
+def _need(buf, nbytes, what):
+    """Refuse a buffer smaller than the bytes the call reads or writes (the
+    library takes plain pointers and cannot check)."""
+    have = _nbytes(buf)
+    if have is not None and have < nbytes:
+        raise ValueError("%s holds %d bytes; the call reads or writes %d" % (what, have, nbytes))
+
+
+def _span(batch, dist, frame):
+    """Elements a batch touches: (batch - 1) * dist + frame (dist 0 = packed)."""
+    return (int(batch) - 1) * (int(dist) or frame) + frame if batch > 0 else 0
+
+
 def _use_torch_stream(L, *bufs):
     for b in bufs:
         if hasattr(b, "is_cuda") and b.is_cuda:
@@ -186,6 +213,9 @@ def kiss_fft(cfg, fin, fout):
 
 def kiss_fft_stride(cfg, fin, fout, fin_stride):
     """kiss_fft_stride (reference kiss_fft.h:134)."""
+    ce, n = _CPX_BYTES[cfg.dtype], cfg.nfft
+    _need(fin, ((n - 1) * int(fin_stride) + 1) * ce, "fin")
+    _need(fout, n * ce, "fout")
     L = cfg.lib
     _use_torch_stream(L, fin, fout)
     L.kiss_fft_cuda_stride(ctypes.c_void_p(cfg.ptr), _ptr(fin)[0], _ptr(fout)[0], int(fin_stride))
@@ -194,6 +224,9 @@ def kiss_fft_stride(cfg, fin, fout, fin_stride):
 
 def kiss_fft_batch(cfg, fin, fout, batch, in_dist=0, out_dist=0):
     """A batch of kiss_fft calls in one launch (distances in complex elements)."""
+    ce, n = _CPX_BYTES[cfg.dtype], cfg.nfft
+    _need(fin, _span(batch, in_dist, n) * ce, "fin")
+    _need(fout, _span(batch, out_dist, n) * ce, "fout")
     L = cfg.lib
     _use_torch_stream(L, fin, fout)
     rc = L.kiss_fft_cuda_batch(ctypes.c_void_p(cfg.ptr), _ptr(fin)[0], _ptr(fout)[0], int(batch), int(in_dist),
@@ -230,6 +263,9 @@ def kiss_fftr_alloc(nfft, inverse_fft=0, dtype="float"):
 
 def kiss_fftr(cfg, timedata, freqdata):
     """kiss_fftr (reference kiss_fftr.h:37)."""
+    ce, n = _CPX_BYTES[cfg.dtype], cfg.nfft
+    _need(timedata, n * ce // 2, "timedata")
+    _need(freqdata, (n // 2 + 1) * ce, "freqdata")
     L = cfg.lib
     _use_torch_stream(L, timedata, freqdata)
     L.kiss_fftr_cuda(ctypes.c_void_p(cfg.ptr), _ptr(timedata)[0], _ptr(freqdata)[0])
@@ -238,6 +274,9 @@ def kiss_fftr(cfg, timedata, freqdata):
 
 def kiss_fftri(cfg, freqdata, timedata):
     """kiss_fftri (reference kiss_fftr.h:43)."""
+    ce, n = _CPX_BYTES[cfg.dtype], cfg.nfft
+    _need(freqdata, (n // 2 + 1) * ce, "freqdata")
+    _need(timedata, n * ce // 2, "timedata")
     L = cfg.lib
     _use_torch_stream(L, timedata, freqdata)
     L.kiss_fftri_cuda(ctypes.c_void_p(cfg.ptr), _ptr(freqdata)[0], _ptr(timedata)[0])
@@ -245,6 +284,10 @@ def kiss_fftri(cfg, freqdata, timedata):
 
 
 def kiss_fftr_batch(cfg, timedata, freqdata, batch, in_dist=0, out_dist=0):
+    """A batch of kiss_fftr calls (distances in reals / bins, 0 = packed)."""
+    ce, n = _CPX_BYTES[cfg.dtype], cfg.nfft
+    _need(timedata, _span(batch, in_dist, n) * ce // 2, "timedata")
+    _need(freqdata, _span(batch, out_dist, n // 2 + 1) * ce, "freqdata")
     L = cfg.lib
     _use_torch_stream(L, timedata, freqdata)
     rc = L.kiss_fftr_cuda_batch(ctypes.c_void_p(cfg.ptr), _ptr(timedata)[0], _ptr(freqdata)[0], int(batch),
@@ -254,6 +297,10 @@ def kiss_fftr_batch(cfg, timedata, freqdata, batch, in_dist=0, out_dist=0):
 
 
 def kiss_fftri_batch(cfg, freqdata, timedata, batch, in_dist=0, out_dist=0):
+    """A batch of kiss_fftri calls (distances in bins / reals, 0 = packed)."""
+    ce, n = _CPX_BYTES[cfg.dtype], cfg.nfft
+    _need(freqdata, _span(batch, in_dist, n // 2 + 1) * ce, "freqdata")
+    _need(timedata, _span(batch, out_dist, n) * ce // 2, "timedata")
     L = cfg.lib
     _use_torch_stream(L, timedata, freqdata)
     rc = L.kiss_fftri_cuda_batch(ctypes.c_void_p(cfg.ptr), _ptr(freqdata)[0], _ptr(timedata)[0], int(batch),
@@ -273,6 +320,11 @@ def kiss_fftnd_alloc(dims, inverse_fft=0, dtype="float"):
 
 def kiss_fftnd(cfg, fin, fout):
     """kiss_fftnd (reference kiss_fftnd.h:21)."""
+    prod = 1
+    for d in cfg.dims:
+        prod *= int(d)
+    _need(fin, prod * _CPX_BYTES[cfg.dtype], "fin")
+    _need(fout, prod * _CPX_BYTES[cfg.dtype], "fout")
     L = cfg.lib
     _use_torch_stream(L, fin, fout)
     L.kiss_fftnd_cuda(ctypes.c_void_p(cfg.ptr), _ptr(fin)[0], _ptr(fout)[0])
@@ -287,8 +339,19 @@ def kiss_fftndr_alloc(dims, inverse_fft=0, dtype="float"):
                dims=list(dims), inverse=int(inverse_fft))
 
 
+def _ndr_need(cfg, timedata, freqdata):
+    ce = _CPX_BYTES[cfg.dtype]
+    prod = 1
+    for d in cfg.dims:
+        prod *= int(d)
+    last = int(cfg.dims[-1])
+    _need(timedata, prod * ce // 2, "timedata")
+    _need(freqdata, prod // last * (last // 2 + 1) * ce, "freqdata")
+
+
 def kiss_fftndr(cfg, timedata, freqdata):
     """kiss_fftndr (reference kiss_fftndr.h:31)."""
+    _ndr_need(cfg, timedata, freqdata)
     L = cfg.lib
     _use_torch_stream(L, timedata, freqdata)
     L.kiss_fftndr_cuda(ctypes.c_void_p(cfg.ptr), _ptr(timedata)[0], _ptr(freqdata)[0])
@@ -297,6 +360,7 @@ def kiss_fftndr(cfg, timedata, freqdata):
 
 def kiss_fftndri(cfg, freqdata, timedata):
     """kiss_fftndri (reference kiss_fftndr.h:40)."""
+    _ndr_need(cfg, timedata, freqdata)
     L = cfg.lib
     _use_torch_stream(L, timedata, freqdata)
     L.kiss_fftndri_cuda(ctypes.c_void_p(cfg.ptr), _ptr(freqdata)[0], _ptr(timedata)[0])
@@ -322,6 +386,7 @@ def kiss_fastfir(cfg, inbuf, outbuf, n_new, offset):
 
     ``offset`` is a one-element list (the in/out ``size_t *offset``).
     Returns the number of output samples written."""
+    _need(inbuf, (int(offset[0]) + int(n_new)) * 4, "inbuf")
     L = cfg.lib
     _use_torch_stream(L, inbuf, outbuf)
     off = ctypes.c_size_t(int(offset[0]))
