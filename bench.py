@@ -658,6 +658,10 @@ def main():
                 "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
+    if rank != 0:
+        # one GPU per run: transforms are independent units, so more GPUs
+        # would be replicas; this bench measures the one on rank 0
+        return
     if args.only:
         import torch
         torch.cuda.set_device(0)
@@ -669,7 +673,7 @@ def main():
     cpu = r["cpu"]
     if rank == 0:
         line = {"metric": "HBM GB/s (compulsory bytes), batched FFT", "value": round(r["value"], 1), "unit": "GB/s",
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms"], 3),
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms"], 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
                 "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
