@@ -8,8 +8,9 @@ produces, under kissfft_gb300/lib/:
                                  type in float, double, int16_t, int32_t
     fftutil_cuda-<type>          the tools/fftutil.c stream front end on the GPU
 
-The kernels are compiled once per (sample type, kernel family) pair from
-csrc/kf_inst.cu, all translation units in parallel, for sm_103a only.
+The kernels are compiled once per (sample type, kernel family, transform
+mode) part from csrc/kf_inst.cu, all translation units in parallel, for
+sm_103a only.
 Objects are cached by a hash of their sources and flags.
 """
 import concurrent.futures as cf
@@ -77,6 +78,22 @@ def fftutil_bin(dtype):
     return os.path.join(LIB, "fftutil_cuda-%s" % dtype)
 
 
+# (sample type, kernel family, transform mode) parts of csrc/kf_inst.cu: one
+# translation unit each, so the build runs them in parallel.  Modes 0..2 are
+# c2c, r2c, c2r; mode 3, the fused fast FIR, exists for float families 0 and 1.
+INST_PARTS = [(dt, fam, mode) for dt in range(4) for fam in range(3) for mode in range(4)
+              if mode < 3 or (dt == 0 and fam < 2)]
+
+
+def _cost(task):
+    """Rough compile-time rank of a task (bigger first)."""
+    name = os.path.basename(task[2])
+    if name.startswith("kf_inst_"):
+        dt, fam, _ = (int(x) for x in name[len("kf_inst_"):-2].split("_"))
+        return (3 if dt == 0 else 1) * (1 + fam)
+    return 0
+
+
 def _digest(paths, flags):
     h = hashlib.sha256()
     for p in paths:
@@ -113,12 +130,11 @@ def build(verbose=False, jobs=None):
     os.makedirs(LIB, exist_ok=True)
     hdrs = _hdrs()
     tasks = []
-    for dt in range(4):
-        for fam in range(3):
-            out = os.path.join(BUILD, "kf_inst_%d_%d.o" % (dt, fam))
-            cmd = [NVCC] + NVFLAGS + ["-DKF_INST_DT=%d" % dt, "-DKF_INST_FAM=%d" % fam, "-c",
-                                      os.path.join(CSRC, "kf_inst.cu"), "-o", out]
-            tasks.append((cmd, [os.path.join(CSRC, "kf_inst.cu")] + hdrs, out))
+    for dt, fam, mode in INST_PARTS:
+        out = os.path.join(BUILD, "kf_inst_%d_%d_%d.o" % (dt, fam, mode))
+        cmd = [NVCC] + NVFLAGS + ["-DKF_INST_DT=%d" % dt, "-DKF_INST_FAM=%d" % fam, "-DKF_INST_MODE=%d" % mode,
+                                  "-c", os.path.join(CSRC, "kf_inst.cu"), "-o", out]
+        tasks.append((cmd, [os.path.join(CSRC, "kf_inst.cu")] + hdrs, out))
     out = os.path.join(BUILD, "kf_lib.o")
     tasks.append(([NVCC] + NVFLAGS + ["-c", os.path.join(CSRC, "kf_lib.cu"), "-o", out],
                   [os.path.join(CSRC, "kf_lib.cu")] + hdrs, out))
@@ -139,8 +155,8 @@ def build(verbose=False, jobs=None):
     out = os.path.join(BUILD, "kf_hdrs_gen.o")
     tasks.append((["g++"] + CXXFLAGS + ["-c", gen, "-o", out], [gen], out))
     jobs = jobs or max(1, os.cpu_count() or 1)
-    # longest first: the general-family units
-    tasks.sort(key=lambda t: 0 if "_2.o" in t[2] else 1)
+    # longest first: float (three-stage register groups), then the general and smooth families
+    tasks.sort(key=_cost, reverse=True)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda t: _compile(t[0], t[1], t[2], verbose), tasks))
     core = core_lib()
