@@ -77,3 +77,25 @@ def test_specialised_kernels_compile(libs, dt, real, n):
     core.kfg_last_error.restype = ctypes.c_char_p
     rc = core.kfg_specialize_check(dt, real, n, 0, ctypes.c_longlong(4096))
     assert rc == 0, core.kfg_last_error().decode()
+
+
+def test_every_kernel_part_linked(libs):
+    """The per-(type, family, mode) kernel units all reach the core library:
+    every launcher the mode dispatchers call is defined there, and nothing of
+    the library's own namespace is left undefined for the loader."""
+    import shutil
+    import subprocess
+    from kissfft_gb300 import build
+    if not shutil.which("nm"):
+        pytest.skip("nm not available")
+    out = subprocess.run(["nm", "-C", build.core_lib()], capture_output=True, text=True, check=True).stdout
+    defined = set(re.findall(r"^\S+ [Tt] kf::(launch_(?:engine|multi)_dt\d_fam\d_m\d)\(", out, flags=re.M))
+    want = set()
+    for dt, fam, mode in build.INST_PARTS:
+        want.add("launch_engine_dt%d_fam%d_m%d" % (dt, fam, mode))
+        if mode < 3:
+            want.add("launch_multi_dt%d_fam%d_m%d" % (dt, fam, mode))
+    assert want <= defined, sorted(want - defined)
+    assert len(build.INST_PARTS) == 4 * 3 * 3 + 2   # every type, family and mode, plus the float fast-FIR parts
+    undef = subprocess.run(["nm", "-C", "-u", build.core_lib()], capture_output=True, text=True, check=True).stdout
+    assert "kf::" not in undef
