@@ -313,7 +313,12 @@ size_t kiss_fastfir_cuda_filter(kiss_fastfir_cuda_cfg cfg, const kiss_fft_scalar
 
 size_t kiss_fastfir_cuda(kiss_fastfir_cuda_cfg cfg, kiss_fft_scalar* inbuf, kiss_fft_scalar* outbuf, size_t n_new,
                          size_t* offset) {
-    if (!check(cfg, H_FIR, "kiss_fastfir_cuda") || !offset) return 0;
+    t_status = 0;
+    if (!check(cfg, H_FIR, "kiss_fastfir_cuda")) return 0;
+    if (!offset) {
+        report("kiss_fastfir_cuda", "offset pointer NULL.");
+        return 0;
+    }
     const size_t ntot = n_new + *offset;
     const long long nfft = cfg->n, ngood = cfg->ngood, L = cfg->ntaps;
     if (n_new == 0) {
@@ -332,8 +337,8 @@ size_t kiss_fastfir_cuda(kiss_fastfir_cuda_cfg cfg, kiss_fft_scalar* inbuf, kiss
     const size_t nwritten = (size_t)(nfull * ngood);
     if (nfull > 0) {
         size_t ny = 0;
-        if (kfg_fir_filter(cfg->plan, (const float*)inbuf, nwritten + (size_t)L - 1, (float*)outbuf, &ny, nullptr) !=
-            KFG_OK) {
+        if (note(kfg_fir_filter(cfg->plan, (const float*)inbuf, nwritten + (size_t)L - 1, (float*)outbuf, &ny,
+                                nullptr)) != KFG_OK) {
             report_last("kiss_fastfir_cuda");
             return 0;
         }
@@ -342,16 +347,20 @@ size_t kiss_fastfir_cuda(kiss_fastfir_cuda_cfg cfg, kiss_fft_scalar* inbuf, kiss
     const size_t keep = ntot - nwritten;
     if (nwritten > 0 && keep > 0) {
         if (is_device(inbuf)) {
+            // through a temporary: the kept tail may overlap the front
             void* tmp = nullptr;
             cudaStream_t st = (cudaStream_t)kfg_get_stream();
-            if (cudaMallocAsync(&tmp, keep * sizeof(kiss_fft_scalar), st) != cudaSuccess ||
-                cudaMemcpyAsync(tmp, inbuf + nwritten, keep * sizeof(kiss_fft_scalar), cudaMemcpyDeviceToDevice, st) !=
-                    cudaSuccess ||
-                cudaMemcpyAsync(inbuf, tmp, keep * sizeof(kiss_fft_scalar), cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+            bool ok = cudaMallocAsync(&tmp, keep * sizeof(kiss_fft_scalar), st) == cudaSuccess;
+            ok = ok && cudaMemcpyAsync(tmp, inbuf + nwritten, keep * sizeof(kiss_fft_scalar), cudaMemcpyDeviceToDevice,
+                                       st) == cudaSuccess;
+            ok = ok && cudaMemcpyAsync(inbuf, tmp, keep * sizeof(kiss_fft_scalar), cudaMemcpyDeviceToDevice, st) ==
+                           cudaSuccess;
+            if (tmp) cudaFreeAsync(tmp, st);
+            if (!ok) {
+                t_status = KFG_ECUDA;
                 report("kiss_fastfir_cuda", "device copy of the kept samples failed");
                 return 0;
             }
-            cudaFreeAsync(tmp, st);
         } else {
             memmove(inbuf, inbuf + nwritten, keep * sizeof(kiss_fft_scalar));
         }
