@@ -185,3 +185,47 @@ def test_column_tiles_on_row_batches(emu, dtype):
     finally:
         emu.emu_force_col(0)
         emu.emu_force(0, 0)
+
+
+def _largest_prime(n):
+    big, q = 1, 2
+    while q * q <= n:
+        while n % q == 0:
+            big, n = q, n // q
+        q += 1
+    return max(big, n) if n > 1 else big
+
+
+def test_uneven_mix_sizes(emu):
+    """A seeded sample of the 20,000-request uneven mix (seed 3): up to 12
+    sizes of every generic-prime class 7..31 and 40 smooth sizes, each run
+    as its own request kind and sample type against the oracle, and every
+    sampled size also as a Q15 complex transform, bit for bit."""
+    mix = inputs.uneven_mix(20000, seed=3)
+    rng = np.random.default_rng(30)
+    classes = {}
+    for k, d, n in mix:
+        big = _largest_prime(n)
+        classes.setdefault(big if big > 5 else 0, []).append((k, d, n))
+    assert sorted(c for c in classes if c) == [7, 11, 13, 17, 19, 23, 29, 31]
+    sample = []
+    for c, reqs in sorted(classes.items()):
+        pick = rng.choice(len(reqs), size=min(len(reqs), 40 if c == 0 else 12), replace=False)
+        sample += [reqs[i] for i in pick]
+    for k, d, n in sample:
+        x = inputs.cpx((1, n), "int16_t", n + 3)
+        y = np.zeros_like(x)
+        assert emu.emu_c2c(DT["int16_t"], n, 0, 0, p(x), p(y), L(1), L(n), L(1), L(n)) == 0
+        assert np.array_equal(y, kfo.fft(x, 0, "int16_t")), n
+        if k == "c2c" and d != "int16_t":
+            x = inputs.cpx((1, n), d, n)
+            y = np.zeros_like(x)
+            assert emu.emu_c2c(DT[d], n, 0, 0, p(x), p(y), L(1), L(n), L(1), L(n)) == 0
+            check(y, lambda: kfo.fft(x, 0, d), x, d, n)
+        elif k == "r2c":
+            t = inputs.real((1, n), d, n)
+            f = kfo.empty_cpx((1, n // 2 + 1), d)
+            assert emu.emu_r2c(DT[d], n, 0, p(t), p(f), L(1)) == 0
+            ex = np.fft.rfft(t.astype(np.float64), axis=-1)
+            e = np.linalg.norm(f - ex) / np.linalg.norm(ex)
+            assert e <= 2e-7 * max(1.0, np.log2(n)), (n, e)
