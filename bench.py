@@ -17,7 +17,10 @@ Printed JSON line (one, on rank 0):
   roofline  the dominant kernel's achieved GB/s (its compulsory bytes per
           launch / its CUDA-event launch time) against the measured HBM peak
   cpu_baseline  the CPU restatement of the reference path (oracle/, OpenMP
-          over transforms) on this host's cores, on a bounded sample
+          over transforms) on this host's cores, on a bounded sample; its
+          "openmp_build" entry times the reference's own OpenMP form
+          (KISSFFT_OPENMP=1: top-level radix legs of each transform in
+          parallel) on a 1/64 sample
   batched_mix  the uneven-size mix (20,000 requests) as one batch replayed
           from a CUDA graph against the plain per-call form
   serving  the serving loop under Poisson arrivals: p50/p99 latency and
@@ -267,7 +270,9 @@ def run_gpu(args):
         nth = kfo.max_threads()
         g, secs, passes = run_cpu(host_in, nth, args.cpu_seconds)
         cpu = {"value": round(g, 3), "unit": "GB/s", "cores": nth, "kind": "port",
-               "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs)}
+               "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs),
+               "form": "OpenMP over the transforms of each batch (one plan per thread)"}
+        cpu["openmp_build"] = legs_entry(host_in, nth, min(3.0, args.cpu_seconds), 1.0 / 64)
     return {"value": value, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e, "clocks": clocks, "cpu": cpu,
             "gpu_launches": args.steps * sum(launches_per_unit), "alg_bytes": alg_bytes,
             "prepare_s": round(t_prep, 2), "mix": mix, "serving": serving, "others": others}
@@ -594,6 +599,35 @@ def run_cpu(host_in, nthreads, min_seconds):
     return tot_bytes / tot_s / 1e9, tot_s, passes
 
 
+def run_cpu_legs(host_in, nthreads, min_seconds, frac=1.0 / 64):
+    """The reference's own OpenMP build as configured (KISSFFT_OPENMP=1):
+    transforms one after the other, the top-level radix legs of each split
+    over OpenMP threads (kiss_fft.c:250-272), on the first ``frac`` of every
+    input batch, whole passes repeated until at least min_seconds; returns
+    the same fields as run_cpu plus the sample's transform count."""
+    from oracle import kfo
+    us = units()
+    parts = [(x[:max(1, int(b * frac))], dt, n, max(1, int(b * frac))) for x, (dt, n, b) in zip(host_in, us)]
+    tot_bytes, tot_s, passes = 0, 0.0, 0
+    while tot_s < min_seconds or passes == 0:
+        for x, dt, n, k in parts:
+            ts = time.perf_counter()
+            kfo.fft_legs(x, 0, dt, nthreads=nthreads)
+            tot_s += time.perf_counter() - ts
+            tot_bytes += 2 * n * ESZ[dt] * k
+        passes += 1
+    return tot_bytes / tot_s / 1e9, tot_s, passes, sum(k for _, _, _, k in parts)
+
+
+def legs_entry(host_in, nthreads, min_seconds, frac, base_frac=1.0):
+    """run_cpu_legs as a JSON object; host_in holds base_frac of every full batch."""
+    g, secs, passes, count = run_cpu_legs(host_in, nthreads, min_seconds, frac)
+    return {"value": round(g, 3), "unit": "GB/s", "cores": nthreads, "kind": "port",
+            "sample": "1/%d of every batch (%d transforms), %d pass(es), %.1f s" % (round(1 / (frac * base_frac)),
+                                                                                      count, passes, secs),
+            "form": "KISSFFT_OPENMP=1: transforms in sequence, top-level radix legs (p <= 5) in parallel"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -654,7 +688,9 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": nth, "kind": "port",
-                                 "sample": sample},
+                                 "sample": sample,
+                                 "form": "OpenMP over the transforms of each batch (one plan per thread)",
+                                 "openmp_build": legs_entry(host_in, nth, 3.0, 1.0 / 8, args.cpu_frac)},
                 "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return

@@ -104,6 +104,21 @@ def fft(x, inverse=False, dtype="float", nthreads=1):
     return out
 
 
+def fft_legs(x, inverse=False, dtype="float", nthreads=1):
+    """Batched complex transform with the reference's KISSFFT_OPENMP split:
+    transforms one after the other, the top-level legs of each in parallel
+    (kiss_fft.c:250-272).  Same results as fft()."""
+    x = as_cpx(x, dtype)
+    n = x.shape[-2] if is_fixed(dtype) else x.shape[-1]
+    batch = x.size // (2 * n if is_fixed(dtype) else n)
+    out = np.empty_like(x)
+    rc = getattr(lib(), "kfo_fft_batch_legs_" + SFX[dtype])(int(n), int(bool(inverse)), _p(x), _p(out),
+                                                             ctypes.c_long(batch), int(nthreads))
+    if rc != 0:
+        raise MemoryError("kfo_fft_batch_legs: scratch allocation failed")
+    return out
+
+
 def fft_stride(x, nfft, stride, inverse=False, dtype="float"):
     """One kiss_fft_stride call: input read at every ``stride``-th element."""
     x = as_cpx(x, dtype)

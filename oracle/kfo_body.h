@@ -273,31 +273,39 @@ static void KFN(plan_free)(PLAN *p) {
     free(p);
 }
 
-/* Depth-first decimation in time, the recursion of kf_work (kiss_fft.c:235-300)
- * without the OpenMP top-level split: the p sub-transforms of length m read
- * the input decimated by fstride*p, then the radix-p butterfly combines them. */
-static void KFN(work)(CPX *out, const CPX *in, size_t fs, int istride, const int *fac, const PLAN *pl) {
-    const int p = fac[0], m = fac[1];
-    if (m == 1) {
-        for (int q = 0; q < p; ++q) out[q] = in[(size_t)q * fs * istride];
-    } else {
-        for (int q = 0; q < p; ++q)
-            KFN(work)(out + q * m, in + (size_t)q * fs * istride, fs * p, istride, fac + 2, pl);
-    }
+/* The radix-p butterfly of one stage (the switch at the end of kf_work,
+ * kiss_fft.c:293-299); scr holds p elements for the generic radix. */
+static void KFN(stage)(CPX *out, size_t fs, int p, int m, const PLAN *pl, CPX *scr) {
     switch (p) {
         case 2: KFN(bf2)(out, fs, pl->tw, m); break;
         case 3: KFN(bf3)(out, fs, pl->tw, m); break;
         case 4: KFN(bf4)(out, fs, pl->tw, m, pl->inverse); break;
         case 5: KFN(bf5)(out, fs, pl->tw, m); break;
-        default: KFN(bfg)(out, fs, pl->tw, m, p, pl->nfft, pl->scr); break;
+        default: KFN(bfg)(out, fs, pl->tw, m, p, pl->nfft, scr); break;
     }
+}
+
+/* Depth-first decimation in time, the recursion of kf_work (kiss_fft.c:235-300)
+ * without the OpenMP top-level split: the p sub-transforms of length m read
+ * the input decimated by fstride*p, then the radix-p butterfly combines them.
+ * scr is the generic butterfly's scratch (the reference mallocs it per
+ * butterfly call, kiss_fft.c:205). */
+static void KFN(work)(CPX *out, const CPX *in, size_t fs, int istride, const int *fac, const PLAN *pl, CPX *scr) {
+    const int p = fac[0], m = fac[1];
+    if (m == 1) {
+        for (int q = 0; q < p; ++q) out[q] = in[(size_t)q * fs * istride];
+    } else {
+        for (int q = 0; q < p; ++q)
+            KFN(work)(out + q * m, in + (size_t)q * fs * istride, fs * p, istride, fac + 2, pl, scr);
+    }
+    KFN(stage)(out, fs, p, m, pl, scr);
 }
 
 /* kiss_fft_stride, kiss_fft.c:375-399 (out-of-place case).  nfft == 1 runs
  * the reference's factor list [1, 1]: a leaf copy and a p = 1 generic
  * butterfly, which in fixed point still scales by SAMP_MAX/1. */
 static void KFN(exec)(const PLAN *pl, const CPX *in, int istride, CPX *out) {
-    KFN(work)(out, in, 1, istride, pl->fac, pl);
+    KFN(work)(out, in, 1, istride, pl->fac, pl, pl->scr);
 }
 
 /* ------------------------------------------------------------ public API */
@@ -327,6 +335,46 @@ void KFN(kfo_fft_batch)(int nfft, int inverse, const CPX *in, CPX *out, long bat
     for (long b = 0; b < batch; ++b) KFN(exec)(pl, in + b * nfft, 1, out + b * nfft);
     KFN(plan_free)(pl);
 #endif
+}
+
+/* A batch of contiguous complex transforms, one after the other, each with
+ * the reference's KISSFFT_OPENMP split (kf_work, kiss_fft.c:250-272): at the
+ * top level (fstride == 1), when p <= 5 and m != 1, the p sub-transforms run
+ * as an OpenMP parallel for and the top stage's butterfly follows the join;
+ * other plans run on one thread.  This is how the reference's OpenMP build
+ * uses the cores (at most p of them per transform); the results equal
+ * kfo_fft_batch's bit for bit.  Returns 0, or -1 when scratch allocation
+ * fails. */
+int KFN(kfo_fft_batch_legs)(int nfft, int inverse, const CPX *in, CPX *out, long batch, int nthreads) {
+    PLAN *pl = KFN(plan_new)(nfft, inverse);
+    const int p = pl->fac[0], m = pl->fac[1];
+    const int split = p <= 5 && m != 1;
+    /* one generic-butterfly scratch per leg: the legs run at once */
+    CPX *scr = split ? (CPX *)malloc(sizeof(CPX) * (size_t)p * (size_t)nfft) : NULL;
+    if (split && !scr) {
+        KFN(plan_free)(pl);
+        return -1;
+    }
+    for (long b = 0; b < batch; ++b) {
+        const CPX *f = in + b * nfft;
+        CPX *F = out + b * nfft;
+        if (!split) {
+            KFN(exec)(pl, f, 1, F);
+            continue;
+        }
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
+#endif
+        for (int k = 0; k < p; ++k)
+            KFN(work)(F + k * m, f + k, (size_t)p, 1, pl->fac + 2, pl, scr + (size_t)k * nfft);
+        KFN(stage)(F, 1, p, m, pl, pl->scr);
+    }
+#ifndef _OPENMP
+    (void)nthreads;
+#endif
+    free(scr);
+    KFN(plan_free)(pl);
+    return 0;
 }
 
 /* Real forward transform, kiss_fftr.c:63-117.  ncfft = nfft/2. */

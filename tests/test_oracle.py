@@ -132,3 +132,18 @@ def test_float_error_within_bound(golden):
             continue
         bound = 2e-7 * max(1.0, np.log2(c["n"]))
         assert c["ref_relerr"] <= bound, c
+
+
+@pytest.mark.parametrize("dtype", ["float", "double", "int16_t", "int32_t"])
+def test_openmp_leg_split_same_bits(dtype):
+    """The reference's KISSFFT_OPENMP form (top-level legs in parallel,
+    kiss_fft.c:250-272) gives the sequential recursion's results bit for bit,
+    including plans whose legs run generic butterflies (3003 = 3*7*11*13) and
+    plans it does not split (p > 5 or a single stage)."""
+    import inputs
+    for n in (2, 4, 7, 12, 480, 1000, 1024, 3003, 17017, 4099):
+        for inv in (0, 1):
+            x = inputs.cpx((3, n), dtype, n + inv)
+            a = kfo.fft(x, inv, dtype)
+            b = kfo.fft_legs(x, inv, dtype, nthreads=4)
+            assert np.array_equal(a, b), (dtype, n, inv)
