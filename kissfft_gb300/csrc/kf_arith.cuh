@@ -21,6 +21,22 @@
 #define KF_HD inline
 #endif
 
+// Overflow hook.  The reference built with CHECK_OVERFLOW warns when a
+// fixed-point C_ADD / C_SUB / C_ADDTO / C_SUBFROM component, or one of
+// kiss_fftr's two DC sums, leaves [SAMP_MIN, SAMP_MAX] (_kiss_fft_guts.h:57-61,
+// kiss_fftr.c:94-95).  The engine marks exactly those operations with
+// KF_OVF_CHECK(S, a, op, b).  It expands to nothing unless the includer
+// defines KF_OVF_NOTE(S, v) (v: the exact sum as long long); the CPU emulator
+// of the engine defines it to count, the CUDA builds do not.
+#if defined(KF_OVF_NOTE)
+#define KF_OVF_CHECK(S, a, op, b)                                                   \
+    do {                                                                            \
+        if constexpr ((S)0.5 == (S)0) KF_OVF_NOTE(S, (long long)(a) op (long long)(b)); \
+    } while (0)
+#else
+#define KF_OVF_CHECK(S, a, op, b) ((void)0)
+#endif
+
 namespace kf {
 
 // float samples (the only type whose plans use three-stage register groups)
@@ -153,8 +169,12 @@ struct ArFixed {
     // |w| <= SMAX, so -w.i fits S and every product is one widening
     // multiply-add; the sums are exact in P (|a*w| < 2^(2*FB)).
     static KF_HD void cmul_acc(W& ar, W& ai, C a, C w) {
-        ar = add(ar, round2(a.r, w.r, a.i, (S)(0 - w.i)));
-        ai = add(ai, round2(a.r, w.i, a.i, w.r));
+        const W tr = round2(a.r, w.r, a.i, (S)(0 - w.i)), ti = round2(a.r, w.i, a.i, w.r);
+        // C_ADDTO's check sees the stored (truncated) running sum and product
+        KF_OVF_CHECK(S, st(ar), +, st(tr));
+        KF_OVF_CHECK(S, st(ai), +, st(ti));
+        ar = add(ar, tr);
+        ai = add(ai, ti);
     }
 };
 
@@ -170,6 +190,8 @@ struct Ar<int32_t> : ArFixed<int32_t, int64_t, 31, 2147483647> {};
 template <typename S>
 KF_HD cpx<S> c_add(cpx<S> a, cpx<S> b) {
     typedef Ar<S> A;
+    KF_OVF_CHECK(S, a.r, +, b.r);
+    KF_OVF_CHECK(S, a.i, +, b.i);
     cpx<S> r;
     r.r = A::st(A::add(a.r, b.r));
     r.i = A::st(A::add(a.i, b.i));
@@ -178,6 +200,8 @@ KF_HD cpx<S> c_add(cpx<S> a, cpx<S> b) {
 template <typename S>
 KF_HD cpx<S> c_sub(cpx<S> a, cpx<S> b) {
     typedef Ar<S> A;
+    KF_OVF_CHECK(S, a.r, -, b.r);
+    KF_OVF_CHECK(S, a.i, -, b.i);
     cpx<S> r;
     r.r = A::st(A::sub(a.r, b.r));
     r.i = A::st(A::sub(a.i, b.i));

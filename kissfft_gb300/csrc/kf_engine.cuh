@@ -640,6 +640,8 @@ KF_HD void split_vals(const KTab& tb, int k, cpx<S> Xk, cpx<S> Xnk, cpx<S>& Fk, 
     typedef cpx<S> C;
     if (k == 0) {
         C dc = Arr::template fixdiv<2>(Xk);
+        KF_OVF_CHECK(S, dc.r, +, dc.i);
+        KF_OVF_CHECK(S, dc.r, -, dc.i);
         Fk.r = Arr::st(Arr::add(dc.r, dc.i));
         Fk.i = 0;
         Fnk.r = Arr::st(Arr::sub(dc.r, dc.i));

@@ -11,7 +11,9 @@
  * this library, as the checker or the timed CPU baseline.  The GPU library
  * never links or calls it.
  *
- * Build: oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp).  Floating
+ * Build: oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp); a second
+ * build with -DKFO_CHECK_OVERFLOW (libkfo_ovf.so) also counts the overflows
+ * the reference's CHECK_OVERFLOW build warns about.  Floating
  * point contraction must stay off: the float and double builds then perform
  * exactly the reference's operation sequence, and the fixed-point twiddle
  * tables (floor(.5 + SAMP_MAX*cos(phase))) round identically at exact ties.
@@ -63,6 +65,20 @@ int kfo_next_fast_size(int n) {
         while (m % 5 == 0) m /= 5;
         if (m <= 1) return n;
     }
+}
+
+/* Overflows counted by the CHECK_OVERFLOW build of the oracle
+ * (libkfo_ovf.so, -DKFO_CHECK_OVERFLOW); always 0 in the plain build. */
+long kfo_overflow_count = 0;
+
+long kfo_overflows_take(void) { return __atomic_exchange_n(&kfo_overflow_count, 0, __ATOMIC_RELAXED); }
+
+int kfo_checks_overflow(void) {
+#ifdef KFO_CHECK_OVERFLOW
+    return 1;
+#else
+    return 0;
+#endif
 }
 
 int kfo_max_threads(void) {

@@ -19,26 +19,67 @@ SFX = {"float": "f32", "double": "f64", "int16_t": "q15", "int32_t": "q31"}
 SCALAR = {"float": np.float32, "double": np.float64, "int16_t": np.int16, "int32_t": np.int32}
 CPLX = {"float": np.complex64, "double": np.complex128}
 
+# the CHECK_OVERFLOW build (-DKFO_CHECK_OVERFLOW): same results, and it
+# counts the fixed-point overflows the reference's CHECK_OVERFLOW warns about
+LIB_OVF_PATH = os.path.join(HERE, "_build", "libkfo_ovf.so")
+
 _lib = None
+_lib_ovf = None
+_override = None  # set by overflows() while it runs
 
 
 def build():
-    """Compile the oracle library with its Makefile (gcc)."""
+    """Compile the oracle libraries with their Makefile (gcc)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def _load(path):
+    if not os.path.exists(path):
+        build()
+    L = ctypes.CDLL(path)
+    L.kfo_fastfir_f32.restype = ctypes.c_long
+    L.kfo_direct_fir_f32.restype = ctypes.c_long
+    L.kfo_fastfir_nfft.restype = ctypes.c_long
+    L.kfo_overflows_take.restype = ctypes.c_long
+    for s in SFX.values():
+        getattr(L, "kfo_fftr_batch_" + s).restype = ctypes.c_int
+    return L
 
 
 def lib():
     global _lib
+    if _override is not None:
+        return _override
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
-        _lib = ctypes.CDLL(LIB_PATH)
-        _lib.kfo_fastfir_f32.restype = ctypes.c_long
-        _lib.kfo_direct_fir_f32.restype = ctypes.c_long
-        _lib.kfo_fastfir_nfft.restype = ctypes.c_long
-        for s in SFX.values():
-            getattr(_lib, "kfo_fftr_batch_" + s).restype = ctypes.c_int
+        _lib = _load(LIB_PATH)
     return _lib
+
+
+def lib_ovf():
+    global _lib_ovf
+    if _lib_ovf is None:
+        _lib_ovf = _load(LIB_OVF_PATH)
+    return _lib_ovf
+
+
+def overflows(fn, *args, **kwargs):
+    """Run ``fn`` (fft, fftr, fftri, fftnd, ...) of this module on the
+    CHECK_OVERFLOW build of the oracle; returns (result, overflow count).
+
+    The count is the number of warnings the reference built with
+    -DCHECK_OVERFLOW prints (_kiss_fft_guts.h:57-61): one per component of a
+    C_ADD / C_SUB / C_ADDTO / C_SUBFROM whose exact sum leaves
+    [SAMP_MIN, SAMP_MAX], plus kiss_fftr's two DC checks (kiss_fftr.c:94-95).
+    Float and double never count (the reference checks fixed point only)."""
+    global _override
+    L = lib_ovf()
+    L.kfo_overflows_take()
+    _override = L
+    try:
+        out = fn(*args, **kwargs)
+    finally:
+        _override = None
+    return out, int(L.kfo_overflows_take())
 
 
 def _p(a):

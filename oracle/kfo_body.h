@@ -73,6 +73,18 @@ static inline CPX KFN(mul_scalar)(CPX c, KFO_S s) {
 }
 /* HALF_OF of _kiss_fft_guts.h:130 (arithmetic shift of the int expression) */
 static inline int32_t KFN(half)(int32_t x) { return x >> 1; }
+/* CHECK_OVERFLOW_OP of _kiss_fft_guts.h:57-61 in the counting build
+ * (KFO_CHECK_OVERFLOW): a sum or difference of two samples, taken in the
+ * product type, outside [SAMP_MIN, SAMP_MAX] counts one overflow where the
+ * reference built with CHECK_OVERFLOW prints one warning. */
+#  ifdef KFO_CHECK_OVERFLOW
+#    define KFO_OVF(a, op, b) KFN(ovf_note)((int64_t)(a) op (int64_t)(b))
+static inline void KFN(ovf_note)(int64_t v) {
+    if (v > KFO_SAMP_MAX || v < -KFO_SAMP_MAX - 1) __atomic_fetch_add(&kfo_overflow_count, 1, __ATOMIC_RELAXED);
+}
+#  else
+#    define KFO_OVF(a, op, b) ((void)0)
+#  endif
 #  define E_ADD(a, b) KFN(w_add)((int32_t)(a), (int32_t)(b))
 #  define E_SUB(a, b) KFN(w_sub)((int32_t)(a), (int32_t)(b))
 #  define E_NEG(a) KFN(w_neg)((int32_t)(a))
@@ -88,6 +100,7 @@ static inline CPX KFN(c_mul)(CPX a, CPX b) {
 }
 static inline CPX KFN(fixdiv)(CPX c, int p) { (void)p; return c; }
 static inline CPX KFN(mul_scalar)(CPX c, KFO_S s) { c.r *= s; c.i *= s; return c; }
+#  define KFO_OVF(a, op, b) ((void)0)
 #  define E_ADD(a, b) ((a) + (b))
 #  define E_SUB(a, b) ((a) - (b))
 #  define E_NEG(a) (-(a))
@@ -95,8 +108,24 @@ static inline CPX KFN(mul_scalar)(CPX c, KFO_S s) { c.r *= s; c.i *= s; return c
 #  define HALF(x) ((x) * (KFO_S)0.5)
 #endif
 
-static inline CPX KFN(c_add)(CPX a, CPX b) { CPX r; r.r = ST(E_ADD(a.r, b.r)); r.i = ST(E_ADD(a.i, b.i)); return r; }
-static inline CPX KFN(c_sub)(CPX a, CPX b) { CPX r; r.r = ST(E_SUB(a.r, b.r)); r.i = ST(E_SUB(a.i, b.i)); return r; }
+/* C_ADD / C_ADDTO and C_SUB / C_SUBFROM (_kiss_fft_guts.h:100-124), the
+ * macros that carry the reference's overflow checks */
+static inline CPX KFN(c_add)(CPX a, CPX b) {
+    CPX r;
+    KFO_OVF(a.r, +, b.r);
+    KFO_OVF(a.i, +, b.i);
+    r.r = ST(E_ADD(a.r, b.r));
+    r.i = ST(E_ADD(a.i, b.i));
+    return r;
+}
+static inline CPX KFN(c_sub)(CPX a, CPX b) {
+    CPX r;
+    KFO_OVF(a.r, -, b.r);
+    KFO_OVF(a.i, -, b.i);
+    r.r = ST(E_SUB(a.r, b.r));
+    r.i = ST(E_SUB(a.i, b.i));
+    return r;
+}
 
 /* ------------------------------------------------------------- twiddles */
 /* kf_cexp / KISS_FFT_COS / KISS_FFT_SIN, _kiss_fft_guts.h:127-145 */
@@ -382,6 +411,8 @@ static void KFN(fftr_core)(const PLAN *sub, const CPX *stw, const KFO_S *t, CPX 
     int ncfft = sub->nfft;
     KFN(exec)(sub, (const CPX *)t, 1, tmp);
     CPX dc = KFN(fixdiv)(tmp[0], 2);
+    KFO_OVF(dc.r, +, dc.i);  /* kiss_fftr.c:94-95 */
+    KFO_OVF(dc.r, -, dc.i);
     f[0].r = ST(E_ADD(dc.r, dc.i));
     f[ncfft].r = ST(E_SUB(dc.r, dc.i));
     f[0].i = 0;
@@ -569,6 +600,7 @@ void KFN(kfo_fftndri)(const int *dims, int ndims, const CPX *f, KFO_S *t) {
 #undef E_NEG
 #undef ST
 #undef HALF
+#undef KFO_OVF
 #undef PROD
 #undef KFO_FRACBITS
 #undef KFO_SAMP_MAX

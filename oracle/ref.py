@@ -53,11 +53,11 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-def fft(x, inverse=False, dtype="float"):
+def fft(x, inverse=False, dtype="float", variant=""):
     x = kfo.as_cpx(x, dtype)
     fixed = kfo.is_fixed(dtype)
     n = x.shape[-2] if fixed else x.shape[-1]
-    L = lib(dtype)
+    L = lib(dtype, variant)
     cfg = L.kiss_fft_alloc(n, int(bool(inverse)), None, None)
     out = np.empty_like(x)
     xf = x.reshape((-1, n, 2) if fixed else (-1, n))
@@ -68,10 +68,10 @@ def fft(x, inverse=False, dtype="float"):
     return out
 
 
-def fftr(t, dtype="float"):
+def fftr(t, dtype="float", variant=""):
     t = np.ascontiguousarray(t, dtype=kfo.SCALAR[dtype])
     n = t.shape[-1]
-    L = lib(dtype)
+    L = lib(dtype, variant)
     cfg = L.kiss_fftr_alloc(n, 0, None, None)
     out = kfo.empty_cpx(t.shape[:-1] + (n // 2 + 1,), dtype)
     tf = t.reshape(-1, n)
@@ -82,11 +82,11 @@ def fftr(t, dtype="float"):
     return out
 
 
-def fftri(f, nfft, dtype="float"):
+def fftri(f, nfft, dtype="float", variant=""):
     f = kfo.as_cpx(f, dtype)
     nb = nfft // 2 + 1
     fixed = kfo.is_fixed(dtype)
-    L = lib(dtype)
+    L = lib(dtype, variant)
     cfg = L.kiss_fftr_alloc(nfft, 1, None, None)
     ff = f.reshape((-1, nb, 2) if fixed else (-1, nb))
     out = np.zeros((ff.shape[0], nfft), kfo.SCALAR[dtype])
@@ -132,6 +132,26 @@ def fftndri(f, dims, dtype="float"):
     L.kiss_fftndri(cfg, _p(f), _p(out))
     _libc.free(cfg)
     return out
+
+
+def overflow_warnings(fn, *args, **kwargs):
+    """Run ``fn`` (fft, fftr or fftri of this module with variant="-ovf": the
+    reference built with -DCHECK_OVERFLOW) and count the overflow warnings it
+    prints on stderr (_kiss_fft_guts.h:57-61).  Returns (result, count)."""
+    import tempfile
+    _libc.fflush(None)
+    saved = os.dup(2)
+    with tempfile.TemporaryFile() as tf:
+        os.dup2(tf.fileno(), 2)
+        try:
+            out = fn(*args, **kwargs)
+        finally:
+            _libc.fflush(None)
+            os.dup2(saved, 2)
+            os.close(saved)
+        tf.seek(0)
+        count = sum(1 for line in tf if b"overflow" in line)
+    return out, count
 
 
 def fastconvr(h, x, tmpdir):

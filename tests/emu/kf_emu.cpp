@@ -8,7 +8,18 @@
 // without a GPU.  It is never part of the shipped library.
 #include <string.h>
 
+#include <limits>
 #include <vector>
+
+// Count the overflows the reference built with CHECK_OVERFLOW would report
+// (_kiss_fft_guts.h:57-61), at the operations the engine marks with
+// KF_OVF_CHECK (kissfft_gb300/csrc/kf_arith.cuh).
+static long long g_overflows = 0;
+template <typename S>
+static inline void emu_ovf_note(long long v) {
+    if (v > (long long)std::numeric_limits<S>::max() || v < (long long)std::numeric_limits<S>::min()) ++g_overflows;
+}
+#define KF_OVF_NOTE(S, v) emu_ovf_note<S>(v)
 
 #include "kf_plan.h"
 #include "kf_runner.cuh"
@@ -139,6 +150,13 @@ static int run_schedule(Schedule& s, const void* in, void* out, const void* firH
 }
 
 extern "C" {
+
+// overflows counted since the last call
+long long emu_overflows_take(void) {
+    const long long n = g_overflows;
+    g_overflows = 0;
+    return n;
+}
 
 void emu_force(int J, int T) {
     g_force_J = J;

@@ -38,6 +38,24 @@ def real(shape, dtype, seed):
     return rng.uniform(-1.0, 1.0, shape).astype(SCALAR[dtype])
 
 
+def extremes(shape, dtype, seed):
+    """Fixed-point samples drawn from the two ends of the range only (SAMP_MIN
+    or SAMP_MAX, each with probability 1/2): the inputs that drive the
+    butterflies' sums out of range, for the overflow-count checks.  ``shape``
+    is the complex shape for (..., 2) arrays or the real shape."""
+    rng = np.random.default_rng(seed)
+    m = IMAX[dtype]
+    return rng.choice(np.array([-m, m - 1], np.int64), size=tuple(shape)).astype(SCALAR[dtype])
+
+
+def named(gen, shape, dtype, seed, complex_):
+    """The input a golden case names: inputs.<gen>(shape, dtype, seed), where
+    ``extremes`` takes the (..., 2) shape for complex data."""
+    if gen == "extremes" and complex_:
+        shape = tuple(shape) + (2,)
+    return globals()[gen](shape, dtype, seed)
+
+
 def sinusoids(batch, n, seed, noise=0.1):
     """Rows of 3 unit sinusoids (random frequency and phase) plus N(0, noise^2)."""
     rng = np.random.default_rng(seed)

@@ -6,6 +6,7 @@ type's twiddle tables and the fast-FIR output must match bit for bit; this
 pins the oracle that the GPU parity tests compare against.
 """
 import hashlib
+import os
 
 import numpy as np
 import pytest
@@ -147,3 +148,33 @@ def test_openmp_leg_split_same_bits(dtype):
             a = kfo.fft(x, inv, dtype)
             b = kfo.fft_legs(x, inv, dtype, nthreads=4)
             assert np.array_equal(a, b), (dtype, n, inv)
+
+
+def _overflow_cases():
+    import json
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "overflow.json")) as f:
+        return json.load(f)["cases"]
+
+
+def test_overflow_counts_match_reference():
+    """The oracle's CHECK_OVERFLOW build counts exactly the warnings the
+    reference built with -DCHECK_OVERFLOW printed (tests/golden/overflow.json),
+    and its outputs hash to the reference's."""
+    import inputs
+    cases = _overflow_cases()
+    assert sum(1 for c in cases if c["overflows"]) >= 40
+    for c in cases:
+        dt, n, b = c["dtype"], c["n"], c["batch"]
+        if c["kind"] == "c2c":
+            x = inputs.named(c["gen"], (b, n), dt, c["seed"], True)
+            y, cnt = kfo.overflows(kfo.fft, x, c["inverse"], dt)
+        elif c["kind"] == "r2c":
+            x = inputs.named(c["gen"], (b, n), dt, c["seed"], False)
+            y, cnt = kfo.overflows(kfo.fftr, x, dt)
+        else:
+            x = inputs.named(c["gen"], (b, n // 2 + 1), dt, c["seed"], True)
+            y, cnt = kfo.overflows(kfo.fftri, x, n, dt)
+        assert cnt == c["overflows"], c
+        assert hashlib.sha256(np.ascontiguousarray(y).tobytes()).hexdigest() == c["sha"], c
+    # the plain build never counts
+    assert kfo.lib().kfo_checks_overflow() == 0 and kfo.lib_ovf().kfo_checks_overflow() == 1
