@@ -75,12 +75,30 @@ void kiss_fft_cuda_free(void *cfg);
 void kiss_fft_cuda_cleanup(void);
 /* kiss_fft_next_fast_size, kiss_fft.h:150 */
 int kiss_fft_cuda_next_fast_size(int n);
+
 /* The loop `for b < batch: kiss_fft(cfg, fin + b*in_dist, fout + b*out_dist)`
  * (the reference's callers, e.g. tools/fftutil.c:30) as one launch.
  * in_dist/out_dist in complex elements, 0 = nfft.  Returns 0 or a negative
  * status (see kissfft_gb300.h). */
 int kiss_fft_cuda_batch(kiss_fft_cuda_cfg cfg, const kiss_fft_cpx *fin, kiss_fft_cpx *fout, long long batch,
                         long long in_dist, long long out_dist);
+
+/* ---- plan cache: kfc.h --------------------------------------------------- */
+/* The plan cache of kfc.h (kfc.c:24-83): the first call for a size builds
+ * the device plan, later calls reuse it.  Keyed by (nfft, direction) per
+ * sample-type library like find_cached_fft, but guarded by a mutex (the
+ * reference's list is not thread-safe, kfc.c:21-22).  Buffers as for
+ * kiss_fft_cuda. */
+/* kfc_fft, kfc.h:43 */
+void kfc_cuda_fft(int nfft, const kiss_fft_cpx *fin, kiss_fft_cpx *fout);
+/* kfc_ifft, kfc.h:45 */
+void kfc_cuda_ifft(int nfft, const kiss_fft_cpx *fin, kiss_fft_cpx *fout);
+/* kfc_cleanup, kfc.h:48: waits for the library stream, then frees every
+ * cached plan */
+void kfc_cuda_cleanup(void);
+/* The number of cached plans (the reference's static ncached, kfc.c:22,
+ * which its KFC_TEST self-test checks, kfc.c:85-109). */
+int kfc_cuda_ncached(void);
 
 /* ---- real 1-D: kiss_fftr.h ---------------------------------------------- */
 typedef struct kiss_fft_cuda_state *kiss_fftr_cuda_cfg;

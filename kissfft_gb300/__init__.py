@@ -108,6 +108,8 @@ def load(dtype="float"):
         L.kiss_fft_cuda_prepare.argtypes = [vp, ll]
         L.kiss_fft_cuda_autotune.argtypes = [vp, ll]
         L.kiss_fft_cuda_last_error.restype = ctypes.c_char_p
+        L.kfc_cuda_fft.argtypes = [i, vp, vp]
+        L.kfc_cuda_ifft.argtypes = [i, vp, vp]
         _libs[dtype] = L
     return _libs[dtype]
 
@@ -241,6 +243,37 @@ def kiss_fft_free(cfg):
 
 def kiss_fft_cleanup():
     pass
+
+
+# ---------------------------------------------------------------- kfc.h
+def _kfc(fn, nfft, fin, fout, dtype):
+    ce = _CPX_BYTES[dtype]
+    _need(fin, int(nfft) * ce, "fin")
+    _need(fout, int(nfft) * ce, "fout")
+    L = load(dtype)
+    _use_torch_stream(L, fin, fout)
+    getattr(L, fn)(int(nfft), _ptr(fin)[0], _ptr(fout)[0])
+    _raise_on_status(L, fn)
+
+
+def kfc_fft(nfft, fin, fout, dtype="float"):
+    """kfc_fft (reference kfc.h:43): forward transform with a cached plan."""
+    _kfc("kfc_cuda_fft", nfft, fin, fout, dtype)
+
+
+def kfc_ifft(nfft, fin, fout, dtype="float"):
+    """kfc_ifft (reference kfc.h:45): inverse transform with a cached plan."""
+    _kfc("kfc_cuda_ifft", nfft, fin, fout, dtype)
+
+
+def kfc_cleanup(dtype="float"):
+    """kfc_cleanup (reference kfc.h:48): frees the cached plans of one sample type."""
+    load(dtype).kfc_cuda_cleanup()
+
+
+def kfc_ncached(dtype="float"):
+    """Number of cached plans of one sample type (the reference's ncached, kfc.c:22)."""
+    return int(load(dtype).kfc_cuda_ncached())
 
 
 def kiss_fft_next_fast_size(n):

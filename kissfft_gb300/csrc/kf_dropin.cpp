@@ -6,6 +6,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include <cuda_runtime.h>
 
 #include "kiss_fft_cuda.h"
@@ -162,6 +166,66 @@ void kiss_fastfir_cuda_free(void* cfg) { free_state(cfg); }
 void kiss_fft_cuda_cleanup(void) {}
 
 int kiss_fft_cuda_next_fast_size(int n) { return kfg_next_fast_size(n); }
+
+}  // extern "C"
+
+namespace {
+
+// The kfc cache of this sample type's library: (nfft, inverse) -> device
+// plan, like find_cached_fft (kfc.c:24-61) but under a mutex.
+std::mutex g_kfc_mu;
+std::map<std::pair<int, int>, kfg_plan*> g_kfc;
+
+void kfc_run(int nfft, int inverse, const kiss_fft_cpx* fin, kiss_fft_cpx* fout, const char* where) {
+    t_status = 0;
+    if (nfft < 1 || !fin || !fout) {
+        report(where, "bad arguments");
+        return;
+    }
+    kfg_plan* p = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_kfc_mu);
+        auto it = g_kfc.find(std::make_pair(nfft, inverse));
+        if (it != g_kfc.end()) {
+            p = it->second;
+        } else {
+            p = kfg_plan_c2c(KF_DROPIN_DTYPE, nfft, inverse);
+            if (p) g_kfc[std::make_pair(nfft, inverse)] = p;
+        }
+    }
+    if (!p) {
+        t_status = KFG_ECUDA;
+        report_last(where);
+        return;
+    }
+    if (note(kfg_exec(p, fin, fout, nullptr)) != KFG_OK) report_last(where);
+}
+
+}  // namespace
+
+extern "C" {
+
+void kfc_cuda_fft(int nfft, const kiss_fft_cpx* fin, kiss_fft_cpx* fout) {
+    kfc_run(nfft, 0, fin, fout, "kfc_cuda_fft");
+}
+
+void kfc_cuda_ifft(int nfft, const kiss_fft_cpx* fin, kiss_fft_cpx* fout) {
+    kfc_run(nfft, 1, fin, fout, "kfc_cuda_ifft");
+}
+
+void kfc_cuda_cleanup(void) {
+    std::lock_guard<std::mutex> lk(g_kfc_mu);
+    if (g_kfc.empty()) return;
+    // transforms enqueued on device buffers may still read the plans
+    kfg_synchronize();
+    for (auto& kv : g_kfc) kfg_plan_free(kv.second);
+    g_kfc.clear();
+}
+
+int kfc_cuda_ncached(void) {
+    std::lock_guard<std::mutex> lk(g_kfc_mu);
+    return (int)g_kfc.size();
+}
 
 kiss_fftr_cuda_cfg kiss_fftr_cuda_alloc(int nfft, int inverse_fft, void* mem, size_t* lenmem) {
     t_status = 0;

@@ -25,7 +25,7 @@ def libs():
 def declared(header):
     txt = open(os.path.join(INC, header)).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    names = re.findall(r"\b(k(?:iss|fg)_[a-z0-9_]+)\s*\(", txt)
+    names = re.findall(r"\b(k(?:iss|fg|fc)_[a-z0-9_]+)\s*\(", txt)
     return sorted(set(names))
 
 
@@ -41,6 +41,7 @@ def test_dropin_exports(libs):
     _, drop = libs
     names = declared("kiss_fft_cuda.h")
     assert "kiss_fft_cuda_alloc" in names and "kiss_fftndri_cuda" in names and "kiss_fastfir_cuda" in names
+    assert "kfc_cuda_fft" in names and "kfc_cuda_cleanup" in names
     for d, L in drop.items():
         for n in names:
             assert hasattr(L, n), (d, n)
@@ -55,6 +56,21 @@ def test_no_cpu_fallback_without_gpu(libs):
     L.kiss_fft_cuda_alloc.restype = ctypes.c_void_p
     assert not L.kiss_fft_cuda_alloc(1024, 0, None, None)   # NULL like a failed kiss_fft_alloc
     assert L.kiss_fft_cuda_status() != 0
+
+
+def test_kfc_fails_loudly_without_gpu(libs):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import numpy as np
+    _, drop = libs
+    L = drop["float"]
+    x = np.zeros(512, np.complex64)
+    y = np.zeros(512, np.complex64)
+    L.kfc_cuda_fft(512, x.ctypes.data_as(ctypes.c_void_p), y.ctypes.data_as(ctypes.c_void_p))
+    assert L.kiss_fft_cuda_status() != 0   # no plan, no CPU fallback
+    assert L.kfc_cuda_ncached() == 0
+    L.kfc_cuda_cleanup()
 
 
 def test_reference_size_rules(libs):

@@ -73,6 +73,38 @@ def test_c2c_host_pointers_single_calls(kf, dtype):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
+def test_kfc_plan_cache(kf, dtype):
+    """kfc_fft / kfc_ifft / kfc_cleanup (reference kfc.c:24-83): the cache
+    sizes of the reference's KFC_TEST sequence (kfc.c:85-109), and results
+    against the oracle on host buffers, bit-identical on device buffers."""
+    n = 512
+    kf.kfc_cleanup(dtype)
+    assert kf.kfc_ncached(dtype) == 0
+    x = inputs.cpx((n,), dtype, 85)
+    y = kfo.empty_cpx((n,), dtype)
+    kf.kfc_fft(n, x, y, dtype)
+    assert kf.kfc_ncached(dtype) == 1
+    y2 = kfo.empty_cpx((n,), dtype)
+    kf.kfc_fft(n, x, y2, dtype)
+    assert kf.kfc_ncached(dtype) == 1
+    z = kfo.empty_cpx((n,), dtype)
+    kf.kfc_ifft(n, x, z, dtype)
+    assert kf.kfc_ncached(dtype) == 2
+    for got, inv in ((y, 0), (y2, 0), (z, 1)):
+        ref = kfo.fft(x, inv, dtype)
+        if fixed(dtype):
+            assert np.array_equal(got, ref), inv
+        else:
+            assert relerr_rows(c128(got, dtype)[None], c128(ref, dtype)[None]) <= 2 * bound(dtype, n), inv
+    yd = empty_dev(y)
+    kf.kfc_fft(n, to_dev(x), yd, dtype)
+    assert np.array_equal(from_dev(yd, y), y)
+    assert kf.kfc_ncached(dtype) == 2
+    kf.kfc_cleanup(dtype)
+    assert kf.kfc_ncached(dtype) == 0
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
 def test_stride(kf, dtype):
     for n, st in [(480, 3), (1024, 2), (3003, 5), (65536, 2)]:
         cfg = kf.kiss_fft_alloc(n, 0, dtype)
