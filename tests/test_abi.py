@@ -115,3 +115,37 @@ def test_every_kernel_part_linked(libs):
     assert len(build.INST_PARTS) == 4 * 3 * 3 + 2   # every type, family and mode, plus the float fast-FIR parts
     undef = subprocess.run(["nm", "-C", "-u", build.core_lib()], capture_output=True, text=True, check=True).stdout
     assert "kf::" not in undef
+
+
+def test_mem_lenmem_protocol(libs):
+    """The placement protocol of kiss_fft_alloc (reference kiss_fft.h:94-115,
+    kiss_fft.c:349-355) on every alloc of every sample type: with mem NULL
+    the call returns NULL and writes the size it needs to *lenmem; a buffer
+    one byte short is refused the same way.  (Placing the cfg in a large
+    enough buffer needs a GPU: tests/test_gpu_parity.py.)"""
+    import numpy as np
+    _, drop = libs
+    dims = (ctypes.c_int * 2)(8, 6)
+    taps = np.ones(31, np.float32)
+    for dt, L in drop.items():
+        calls = {
+            "kiss_fft_cuda_alloc": lambda m, ln: L.kiss_fft_cuda_alloc(480, 0, m, ln),
+            "kiss_fftr_cuda_alloc": lambda m, ln: L.kiss_fftr_cuda_alloc(480, 0, m, ln),
+            "kiss_fftnd_cuda_alloc": lambda m, ln: L.kiss_fftnd_cuda_alloc(dims, 2, 0, m, ln),
+            "kiss_fftndr_cuda_alloc": lambda m, ln: L.kiss_fftndr_cuda_alloc(dims, 2, 0, m, ln),
+        }
+        if dt == "float":
+            calls["kiss_fastfir_cuda_alloc"] = lambda m, ln: L.kiss_fastfir_cuda_alloc(
+                taps.ctypes.data_as(ctypes.c_void_p), 31, None, m, ln)
+        sizes = set()
+        for name, call in calls.items():
+            getattr(L, name).restype = ctypes.c_void_p
+            need = ctypes.c_size_t(0)
+            assert not call(None, ctypes.byref(need)), (dt, name)
+            assert need.value > 0, (dt, name)
+            sizes.add(need.value)
+            short = ctypes.create_string_buffer(need.value - 1)
+            got = ctypes.c_size_t(need.value - 1)
+            assert not call(short, ctypes.byref(got)), (dt, name)
+            assert got.value == need.value, (dt, name)
+        assert len(sizes) == 1  # one host handle layout for every kind

@@ -73,6 +73,35 @@ def test_c2c_host_pointers_single_calls(kf, dtype):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
+def test_cfg_in_caller_memory(kf, dtype):
+    """kiss_fft_alloc's placement protocol (reference kiss_fft.h:94-115): a
+    size query, then the cfg placed in the caller's buffer (the returned
+    pointer is that buffer), a correct transform through it, and a free that
+    releases the device plan but leaves the buffer to the caller."""
+    import ctypes
+    L = kf.load(dtype)
+    n = 480
+    need = ctypes.c_size_t(0)
+    assert not L.kiss_fft_cuda_alloc(n, 0, None, ctypes.byref(need))
+    buf = ctypes.create_string_buffer(need.value + 64)
+    got = ctypes.c_size_t(len(buf))
+    cfg = L.kiss_fft_cuda_alloc(n, 0, buf, ctypes.byref(got))
+    assert cfg == ctypes.addressof(buf), kf.last_error(dtype)
+    assert got.value == need.value
+    x = inputs.cpx((n,), dtype, 94)
+    y = kfo.empty_cpx((n,), dtype)
+    L.kiss_fft_cuda(ctypes.c_void_p(cfg), x.ctypes.data_as(ctypes.c_void_p), y.ctypes.data_as(ctypes.c_void_p))
+    assert L.kiss_fft_cuda_status() == 0
+    ref = kfo.fft(x, 0, dtype)
+    if fixed(dtype):
+        assert np.array_equal(y, ref)
+    else:
+        assert relerr_rows(c128(y, dtype)[None], c128(ref, dtype)[None]) <= 2 * bound(dtype, n)
+    L.kiss_fft_cuda_free(ctypes.c_void_p(cfg))
+    del buf
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
 def test_kfc_plan_cache(kf, dtype):
     """kfc_fft / kfc_ifft / kfc_cleanup (reference kfc.c:24-83): the cache
     sizes of the reference's KFC_TEST sequence (kfc.c:85-109), and results
