@@ -11,7 +11,9 @@ all 12 (type, size) batches once.  Every input batch is larger than the
 
 Printed JSON line (one, on rank 0):
   value   whole-job HBM throughput, GB/s of compulsory bytes
-          (2*N*sizeof(complex) per transform), inputs resident in HBM
+          (2*N*sizeof(complex) per transform), inputs resident in HBM;
+          gflops_5nlog2n gives the same run (and each unit) as
+          5*N*log2(N) operations per transform
   e2e     the same through the drop-in C ABI with host (pinned) buffers,
           host<->device copies inside the timed region
   roofline  the dominant kernel's achieved GB/s (its compulsory bytes per
@@ -53,6 +55,13 @@ BATCH_BYTES = 256 * 1024 * 1024
 # launches (profiles/ncu_dram_traffic_3003.md, profiles/ncu_engine_kernels_bench_sizes.md);
 # the write figure misses the dirty lines still in L2 when the capture ends
 NCU_TRAFFIC = {("int16_t", 3003, 22347): 486.0e6, ("int32_t", 3003, 11173): 483.2e6, ("float", 1000, 33554): 485.8e6}
+
+
+def c2c_flops(n, b):
+    """Nominal operations of b complex transforms of n points: 5*n*log2(n)
+    each, the usual FFT operation count (for Q15/Q31 these are integer
+    operations counted the same way)."""
+    return 5.0 * n * float(np.log2(n)) * b if n > 1 else 0.0
 
 
 def peaks():
@@ -204,7 +213,9 @@ def run_gpu(args):
     for i, (dt, n, b) in enumerate(us):
         byts = 2 * n * ESZ[dt] * b
         unit_rows.append({"dtype": dt, "nfft": n, "batch": b, "ms": round(per[i], 4),
-                          "gbs": round(byts / (per[i] * 1e-3) / 1e9, 1), "launches": launches_per_unit[i]})
+                          "gbs": round(byts / (per[i] * 1e-3) / 1e9, 1),
+                          "gflops_5nlog2n": round(c2c_flops(n, b) / (per[i] * 1e-3) / 1e9, 1),
+                          "launches": launches_per_unit[i]})
     dom = max(range(len(us)), key=lambda i: per[i])
     peak, peak_kind = peaks()
     dt_, n_, b_ = us[dom]
@@ -273,7 +284,9 @@ def run_gpu(args):
                "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs),
                "form": "OpenMP over the transforms of each batch (one plan per thread)"}
         cpu["openmp_build"] = legs_entry(host_in, nth, min(3.0, args.cpu_seconds), 1.0 / 64)
-    return {"value": value, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e, "clocks": clocks, "cpu": cpu,
+    gflops = sum(c2c_flops(n, b) for dt, n, b in us) / (ms * 1e-3) / 1e9
+    return {"value": value, "gflops": gflops, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e,
+            "clocks": clocks, "cpu": cpu,
             "gpu_launches": args.steps * sum(launches_per_unit), "alg_bytes": alg_bytes,
             "prepare_s": round(t_prep, 2), "mix": mix, "serving": serving, "others": others}
 
@@ -709,6 +722,7 @@ def main():
     cpu = r["cpu"]
     if rank == 0:
         line = {"metric": "HBM GB/s (compulsory bytes), batched FFT", "value": round(r["value"], 1), "unit": "GB/s",
+                "gflops_5nlog2n": round(r["gflops"], 1),
                 "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms"], 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,

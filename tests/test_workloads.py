@@ -59,3 +59,11 @@ def test_uneven_mix_sizes_build_plans():
     for k, d, n in set(inputs.uneven_mix(20000, seed=3)):
         dt = 0 if d == "float" else 2
         assert E.emu_plan_info(dt, n // 2 if k == "r2c" else n, 0, out) == 0, (k, d, n)
+
+
+def test_bench_operation_count():
+    """bench.py's GFLOP/s figures count 5*N*log2(N) per complex transform."""
+    import bench
+    assert bench.c2c_flops(1024, 2) == 2 * 5 * 1024 * 10
+    assert bench.c2c_flops(480, 1) == 5 * 480 * np.log2(480)
+    assert bench.c2c_flops(1, 7) == 0
