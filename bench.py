@@ -14,6 +14,10 @@ Printed JSON line (one, on rank 0):
           (2*N*sizeof(complex) per transform), inputs resident in HBM;
           gflops_5nlog2n gives the same run (and each unit) as
           5*N*log2(N) operations per transform
+  accuracy  the outputs of the timed launches, first 64 transforms of every
+          unit: float worst relative L2 error against FP64 beside the
+          reference float build's own error on the same rows; Q15/Q31
+          bit-exactness against the reference's fixed-point arithmetic
   e2e     the same through the drop-in C ABI with host (pinned) buffers,
           host<->device copies inside the timed region
   roofline  the dominant kernel's achieved GB/s (its compulsory bytes per
@@ -62,6 +66,51 @@ def c2c_flops(n, b):
     each, the usual FFT operation count (for Q15/Q31 these are integer
     operations counted the same way)."""
     return 5.0 * n * float(np.log2(n)) * b if n > 1 else 0.0
+
+
+def device_rows(t, dt, n, k):
+    """The first k transforms of a bench buffer (a torch tensor laid out as
+    the bench uploads it: float32 (b, 2n) for float, (b, n, 2) integers for
+    Q15/Q31) as a numpy array in the oracle's layout."""
+    a = t[:k].cpu().numpy()
+    if dt == "float":
+        return a.view(np.complex64).reshape(k, n)
+    return a.reshape(k, n, 2)
+
+
+def accuracy(dt, n, x, y):
+    """Accuracy of forward transforms y of the rows x: for float the worst
+    per-row relative L2 error against an FP64 transform, beside the same for
+    the reference float build's own output (the oracle, bit-identical to
+    it) and the bound 2e-7*log2(n); for Q15/Q31 bit-exactness against the
+    oracle (the reference's fixed-point build)."""
+    from oracle import kfo
+    ref = kfo.fft(x, 0, dt)
+    if dt in ("int16_t", "int32_t"):
+        return {"rows": int(x.shape[0]), "bit_exact": bool(np.array_equal(y, ref))}
+    exact = np.fft.fft(x.astype(np.complex128), axis=-1)
+    scale = np.linalg.norm(exact, axis=-1)
+    scale[scale == 0] = 1
+
+    def worst(a):
+        return float(np.max(np.linalg.norm(a.astype(np.complex128) - exact, axis=-1) / scale))
+    return {"rows": int(x.shape[0]), "relerr": worst(y), "ref_relerr": worst(ref),
+            "bound": 2e-7 * max(1.0, float(np.log2(n)))}
+
+
+def accuracy_summary(unit_rows):
+    """The worst float error (and the reference float build's on the same
+    rows) and whether every Q15/Q31 unit was bit-exact."""
+    fl = [u["accuracy"] for u in unit_rows if "relerr" in u.get("accuracy", {})]
+    fx = [u["accuracy"] for u in unit_rows if "bit_exact" in u.get("accuracy", {})]
+    out = {"rows_per_unit": max([a["rows"] for a in fl + fx] or [0])}
+    if fl:
+        out["float_worst_relerr"] = max(a["relerr"] for a in fl)
+        out["float_ref_worst_relerr"] = max(a["ref_relerr"] for a in fl)
+        out["float_within_bound"] = all(a["relerr"] <= a["bound"] for a in fl)
+    if fx:
+        out["fixed_bit_exact"] = all(a["bit_exact"] for a in fx)
+    return out
 
 
 def peaks():
@@ -216,6 +265,10 @@ def run_gpu(args):
                           "gbs": round(byts / (per[i] * 1e-3) / 1e9, 1),
                           "gflops_5nlog2n": round(c2c_flops(n, b) / (per[i] * 1e-3) / 1e9, 1),
                           "launches": launches_per_unit[i]})
+    # accuracy of the outputs just timed, on the first 64 transforms of every unit
+    for i, (dt, n, b) in enumerate(us):
+        k = min(b, 64)
+        unit_rows[i]["accuracy"] = accuracy(dt, n, host_in[i][:k], device_rows(ys[i], dt, n, k))
     dom = max(range(len(us)), key=lambda i: per[i])
     peak, peak_kind = peaks()
     dt_, n_, b_ = us[dom]
@@ -726,6 +779,7 @@ def main():
                 "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms"], 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+q15+q31",
                 "data": "synthetic", "config": config, "roofline": r["roofline"], "cpu_baseline": cpu,
+                "accuracy": accuracy_summary(r["units"]),
                 "e2e": r["e2e"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "units": r["units"],
                 "batched_mix": r["mix"], "serving": r["serving"], "other_configs": r["others"],
                 "kernels": ("plan-specialised (NVRTC)" if args.specialize else "precompiled families") +

@@ -67,3 +67,32 @@ def test_bench_operation_count():
     assert bench.c2c_flops(1024, 2) == 2 * 5 * 1024 * 10
     assert bench.c2c_flops(480, 1) == 5 * 480 * np.log2(480)
     assert bench.c2c_flops(1, 7) == 0
+
+
+def test_bench_accuracy_helpers():
+    """bench.py's accuracy fields: the device-buffer row view, the float error
+    beside the reference float build's, fixed-point bit-exactness, and the
+    summary (run here on CPU tensors laid out as the bench uploads them)."""
+    import torch
+
+    import bench
+    rows = []
+    for dt, n in (("float", 480), ("int16_t", 1000), ("int32_t", 3003)):
+        x = inputs.cpx((5, n), dt, n)
+        xv = x.view(np.float32) if dt == "float" else x
+        t = torch.from_numpy(np.ascontiguousarray(xv))
+        back = bench.device_rows(t, dt, n, 3)
+        assert np.array_equal(back, x[:3])
+        from oracle import kfo
+        y = kfo.fft(x[:3], 0, dt)
+        a = bench.accuracy(dt, n, x[:3], y)
+        if dt == "float":
+            assert a["relerr"] == a["ref_relerr"] and a["relerr"] <= a["bound"]
+        else:
+            assert a["bit_exact"]
+            y2 = y.copy()
+            y2[0, 0, 0] ^= 1
+            assert not bench.accuracy(dt, n, x[:3], y2)["bit_exact"]
+        rows.append({"accuracy": a})
+    s = bench.accuracy_summary(rows)
+    assert s["fixed_bit_exact"] and s["float_within_bound"] and s["rows_per_unit"] == 3
