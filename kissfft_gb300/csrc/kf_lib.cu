@@ -379,8 +379,9 @@ void apply_cfgs(Schedule& s, const std::vector<std::array<int, 5>>& v) {
         if (c[3] && !st.args.col_in) recolumn_step(st);
         if (c[0] != st.cfg.J) reshape_step(st, c[0]);
         if (c[4] && c[4] != st.cfg.T) retarget_threads(st, c[4]);
-        st.cfg.minb = c[1];
-        st.tma_ok = c[2];
+        // the tuning file is plain text on disk: take only budgets a launch can have
+        if (c[1] >= 1 && c[1] <= 32) st.cfg.minb = c[1];
+        st.tma_ok = c[2] != 0;
     }
 }
 
