@@ -8,7 +8,8 @@
  * Each function cites the reference file:line it restates.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
- * this library, as the checker or the timed CPU baseline.  The GPU library
+ * this library, as the results to compare against or the timed CPU
+ * baseline.  The GPU library
  * never links or calls it.
  *
  * Build: oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp); a second

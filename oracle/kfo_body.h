@@ -9,8 +9,8 @@
  *     KFO_SFX    name suffix (f32, f64, q15, q31)
  *
  * It is used only by the test suite, by __graft_entry__.smoke() and by the
- * CPU-baseline leg of bench.py, always as the checker or the timed CPU
- * baseline -- never as part of the shipped GPU path.
+ * CPU-baseline leg of bench.py, always as the results to compare against
+ * or the timed CPU baseline -- never as part of the shipped GPU path.
  *
  * Fixed-point model (reference _kiss_fft_guts.h:43-82, 100-130): every value
  * stored into a sample variable is truncated to the storage width; every

@@ -1,8 +1,8 @@
 """Seeded synthetic inputs shared by the golden-fixture generator and the tests.
 
 numpy's PCG64 ``default_rng`` streams are identical on every platform, so
-the same (kind, dtype, shape, seed) reproduces the same bytes here and on the
-GPU host.  Value distributions follow the workload descriptions:
+the same (kind, dtype, shape, seed) reproduces the same bytes on every
+machine (x86-64 and aarch64 alike).  Value distributions follow the workload descriptions:
 complex IEEE inputs have re/im i.i.d. uniform[-1, 1); fixed-point inputs are
 uniform over the full integer range.
 """

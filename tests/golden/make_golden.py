@@ -1,6 +1,7 @@
 """Generate the golden fixtures from the reference library built from source.
 
-Run where the reference tree is present (it is not on the GPU host):
+Run where the reference tree is present (the tests read the files it writes
+anywhere, with or without the reference):
 
     python tests/golden/make_golden.py
 

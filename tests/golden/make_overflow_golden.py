@@ -1,7 +1,8 @@
 """Generate tests/golden/overflow.json from the reference built with its
 overflow warnings on.
 
-Run where the reference tree is present (it is not on the GPU host):
+Run where the reference tree is present (the tests read the file it writes
+anywhere, with or without the reference):
 
     python tests/golden/make_overflow_golden.py
 
