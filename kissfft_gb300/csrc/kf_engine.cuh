@@ -42,8 +42,19 @@ union KfPun {
     T t;
 };
 
+// Memory-access hook: every shared-tile, global-buffer and table access of
+// the engine is marked with KF_MEM_CHECK(p, bytes).  It expands to nothing
+// unless the includer defines KF_MEM_NOTE(p, bytes); the CPU emulator of the
+// engine does, and checks each access against the buffers of its run.
+#if defined(KF_MEM_NOTE)
+#define KF_MEM_CHECK(p, n) KF_MEM_NOTE((const void*)(p), (size_t)(n))
+#else
+#define KF_MEM_CHECK(p, n) ((void)0)
+#endif
+
 template <typename T>
 KF_HD T ldro(const T* p) {
+    KF_MEM_CHECK(p, sizeof(T));
 #if defined(__CUDA_ARCH__)
     if constexpr (sizeof(T) == 4) {
         KfPun<T, unsigned> u;
@@ -82,6 +93,7 @@ struct KfVec {
 // min(16, W*sizeof(cpx)) bytes.
 template <typename S, int W>
 KF_HD void ldro_vec(const cpx<S>* p, cpx<S>* out) {
+    KF_MEM_CHECK(p, W * sizeof(cpx<S>));
 #if defined(__CUDA_ARCH__)
     typename KfVec<S, W>::U u;
     constexpr int bytes = KfVec<S, W>::bytes;
@@ -135,8 +147,8 @@ struct Tile {
     int* err;
 
     KF_HD int sidx(int A, int job) const { return swz<S>(A * sA + job * sJ); }
-    KF_HD C sld(int A, int job) const { return sm[sidx(A, job)]; }
-    KF_HD void sst(int A, int job, C v) const { sm[sidx(A, job)] = v; }
+    KF_HD C sld(int A, int job) const { return (KF_MEM_CHECK(sm + sidx(A, job), sizeof(C)), sm[sidx(A, job)]); }
+    KF_HD void sst(int A, int job, C v) const { (KF_MEM_CHECK(sm + sidx(A, job), sizeof(C)), sm[sidx(A, job)] = v); }
     KF_HD bool valid(int job) const { return inb[job] >= 0; }
 };
 
@@ -153,10 +165,10 @@ struct GIn {
         cpx<S> v;
         if constexpr (MODE == MODE_FIR) {
             const long long i0 = 2LL * off;
-            v.r = i0 < lim ? r[i0] : (S)0;
-            v.i = i0 + 1 < lim ? r[i0 + 1] : (S)0;
+            v.r = i0 < lim ? (KF_MEM_CHECK(r + i0, sizeof(S)), r[i0]) : (S)0;
+            v.i = i0 + 1 < lim ? (KF_MEM_CHECK(r + i0 + 1, sizeof(S)), r[i0 + 1]) : (S)0;
         } else {
-            v = p[(long long)(off * stride)];
+            v = (KF_MEM_CHECK(p + (long long)(off * stride), sizeof(v)), p[(long long)(off * stride)]);
         }
         return v;
     }
@@ -187,10 +199,10 @@ struct GOut {
     KF_HD void st(int off, cpx<S> v) const {
         if constexpr (MODE == MODE_FIR) {
             const long long i0 = 2LL * off;
-            if (i0 < lim) r[i0] = v.r;
-            if (i0 + 1 < lim) r[i0 + 1] = v.i;
+            if (i0 < lim) (KF_MEM_CHECK(r + i0, sizeof(S)), r[i0] = v.r);
+            if (i0 + 1 < lim) (KF_MEM_CHECK(r + i0 + 1, sizeof(S)), r[i0 + 1] = v.i);
         } else {
-            p[(long long)(off * stride)] = v;
+            (KF_MEM_CHECK(p + (long long)(off * stride), sizeof(v)), p[(long long)(off * stride)] = v);
         }
     }
 };
@@ -720,8 +732,8 @@ KF_HD void r2c_post(const Tile<S>& t, const KSub& sb, const KTab& tb, int tid, i
         cpx<S> Fk, Fnk;
         r2c_split_pair(t, sb, tb, job, k, Fk, Fnk);
         cpx<S>* o = (cpx<S>*)t.out + t.outb[job];
-        if (k != ncfft - k) o[(long long)k * t.out_stride] = Fk;
-        o[(long long)(ncfft - k) * t.out_stride] = Fnk;
+        if (k != ncfft - k) (KF_MEM_CHECK(o + (long long)k * t.out_stride, sizeof(Fk)), o[(long long)k * t.out_stride] = Fk);
+        (KF_MEM_CHECK(o + (long long)(ncfft - k) * t.out_stride, sizeof(Fnk)), o[(long long)(ncfft - k) * t.out_stride] = Fnk);
     }
 }
 
@@ -734,8 +746,9 @@ KF_HD void c2r_pre(const Tile<S>& t, const KSub& sb, const KTab& tb, int tid, in
         item_decode(t.J, t.logJ, t.col, nk, it, job, k);
         if (!t.valid(job)) continue;
         const cpx<S>* f = (const cpx<S>*)t.in + t.inb[job];
-        cpx<S> Gk = f[(long long)k * t.in_stride];
-        cpx<S> Gnk = f[(long long)(ncfft - k) * t.in_stride];
+        cpx<S> Gk = (KF_MEM_CHECK(f + (long long)k * t.in_stride, sizeof(cpx<S>)), f[(long long)k * t.in_stride]);
+        cpx<S> Gnk = (KF_MEM_CHECK(f + (long long)(ncfft - k) * t.in_stride, sizeof(cpx<S>)),
+                      f[(long long)(ncfft - k) * t.in_stride]);
         cpx<S> tk, tnk;
         c2r_merge_pair(tb, k, Gk, Gnk, tk, tnk);
         if (k == 0) {
@@ -804,9 +817,11 @@ KF_HD void split_item(const KArgs& a, long long it) {
     const cpx<S>* X = (const cpx<S>*)a.in + (a.in_off ? a.in_off[b] : b * a.in_dhi);
     cpx<S>* F = (cpx<S>*)a.out + (a.out_off ? a.out_off[b] : b * a.out_dhi);
     cpx<S> Fk, Fnk;
+    KF_MEM_CHECK(X + k, sizeof(Fk));
+    KF_MEM_CHECK(X + (k == 0 ? 0 : ncfft - k), sizeof(Fk));
     split_vals(a.tab[0], k, X[k], k == 0 ? X[0] : X[ncfft - k], Fk, Fnk);
-    if (k != ncfft - k) F[k] = Fk;
-    F[ncfft - k] = Fnk;
+    if (k != ncfft - k) (KF_MEM_CHECK(F + k, sizeof(Fk)), F[k] = Fk);
+    (KF_MEM_CHECK(F + ncfft - k, sizeof(Fnk)), F[ncfft - k] = Fnk);
 }
 
 template <typename S>
@@ -817,12 +832,14 @@ KF_HD void merge_item(const KArgs& a, long long it) {
     const cpx<S>* G = (const cpx<S>*)a.in + (a.in_off ? a.in_off[b] : b * a.in_dhi);
     cpx<S>* X = (cpx<S>*)a.out + (a.out_off ? a.out_off[b] : b * a.out_dhi);
     cpx<S> tk, tnk;
+    KF_MEM_CHECK(G + k, sizeof(tk));
+    KF_MEM_CHECK(G + ncfft - k, sizeof(tk));
     c2r_merge_pair(a.tab[0], k, G[k], G[ncfft - k], tk, tnk);
     if (k == 0) {
-        X[0] = tk;
+        (KF_MEM_CHECK(X, sizeof(tk)), X[0] = tk);
     } else {
-        if (k != ncfft - k) X[k] = tk;
-        X[ncfft - k] = tnk;
+        if (k != ncfft - k) (KF_MEM_CHECK(X + k, sizeof(tk)), X[k] = tk);
+        (KF_MEM_CHECK(X + ncfft - k, sizeof(tnk)), X[ncfft - k] = tnk);
     }
 }
 

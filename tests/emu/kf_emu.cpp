@@ -21,6 +21,39 @@ static inline void emu_ovf_note(long long v) {
 }
 #define KF_OVF_NOTE(S, v) emu_ovf_note<S>(v)
 
+// Bounds checking of every access the engine marks with KF_MEM_CHECK
+// (kissfft_gb300/csrc/kf_engine.cuh): an access must lie wholly inside one
+// of the memory regions the current run owns (the caller's input and
+// output, the schedule's scratch, the shared tile of exactly the launch's
+// dynamic size, the plan tables, the fast-FIR response).
+struct EmuRegion {
+    const unsigned char* lo;
+    const unsigned char* hi;
+};
+static std::vector<EmuRegion> g_regions;
+static long long g_oob = 0;
+static inline void emu_mem_note(const void* p, size_t n) {
+    const unsigned char* a = (const unsigned char*)p;
+    for (size_t i = g_regions.size(); i-- > 0;)
+        if (a >= g_regions[i].lo && a + n <= g_regions[i].hi) return;
+    ++g_oob;
+}
+#define KF_MEM_NOTE(p, n) emu_mem_note(p, n)
+
+// Bytes by which the next runs under-declare the output region (which 1) or
+// the shared tile (which 2), to show that the check catches the last
+// accesses; the buffers themselves keep their full size.
+static long long g_trim_out = 0, g_trim_sm = 0;
+static size_t trimmed(size_t n, long long t) { return t > 0 && (size_t)t < n ? n - (size_t)t : n; }
+
+// A region owned for the lifetime of the guard.
+struct EmuOwn {
+    EmuOwn(const void* p, size_t n) {
+        g_regions.push_back({(const unsigned char*)p, (const unsigned char*)p + n});
+    }
+    ~EmuOwn() { g_regions.pop_back(); }
+};
+
 #include "kf_plan.h"
 #include "kf_runner.cuh"
 
@@ -61,6 +94,7 @@ static int run_engine_step_f(const Step& st) {
     const KArgs& a = st.args;
     const LaunchCfg& c = st.cfg;
     std::vector<cpx<S>> sm(c.smem / sizeof(cpx<S>) + 1);
+    EmuOwn own_sm(sm.data(), trimmed((size_t)c.smem, g_trim_sm));
     long long inb[KF_MAXJ], outb[KF_MAXJ], lin[KF_MAXJ], lout[KF_MAXJ];
     int U[KF_MAXJ];
     int err = 0;
@@ -116,6 +150,7 @@ static int run_step_t(const Step& st) {
 
 static int run_schedule(Schedule& s, const void* in, void* out, const void* firH = nullptr) {
     std::vector<uint8_t> tmp(s.scratch[0] + s.scratch[1] + 16);
+    EmuOwn own_s0(tmp.data(), s.scratch[0]), own_s1(tmp.data() + s.scratch[0], s.scratch[1]);
     for (auto& st : s.steps) {
         void* roles[4] = {(void*)in, out, tmp.data(), tmp.data() + s.scratch[0]};
         st.args.in = roles[st.in_role];
@@ -151,6 +186,18 @@ static int run_schedule(Schedule& s, const void* in, void* out, const void* firH
 
 extern "C" {
 
+void emu_trim(int which, long long bytes) {
+    if (which == 1) g_trim_out = bytes;
+    if (which == 2) g_trim_sm = bytes;
+}
+
+// out-of-bounds accesses counted since the last call
+long long emu_oob_take(void) {
+    const long long n = g_oob;
+    g_oob = 0;
+    return n;
+}
+
 // overflows counted since the last call
 long long emu_overflows_take(void) {
     const long long n = g_overflows;
@@ -173,6 +220,11 @@ int emu_c2c(int dtype, int n, int inverse, int lmax, const void* in, void* out, 
     p.bind(p.blob.data());
     Schedule s;
     if (!schedule_c2c(p, batch, in_dist, in_stride, out_dist, s)) return -3;
+    const long long esz = cpx_size(dtype);
+    const long long ind = in_dist ? in_dist : (long long)n * in_stride, outd = out_dist ? out_dist : n;
+    EmuOwn own_p(p.blob.data(), p.blob.size());
+    EmuOwn own_i(in, (size_t)(((batch - 1) * ind + (long long)(n - 1) * in_stride + 1) * esz));
+    EmuOwn own_o(out, trimmed((size_t)(((batch - 1) * outd + n) * esz), g_trim_out));
     return run_schedule(s, in, out);
 }
 
@@ -182,6 +234,10 @@ int emu_r2c(int dtype, int nfft, int lmax, const void* in, void* out, long long 
     p.bind(p.blob.data());
     Schedule s;
     if (!schedule_r2c(p, batch, nfft, nfft / 2 + 1, s)) return -3;
+    const long long esz = cpx_size(dtype);
+    EmuOwn own_p(p.blob.data(), p.blob.size());
+    EmuOwn own_i(in, (size_t)(batch * nfft * esz / 2));
+    EmuOwn own_o(out, (size_t)(batch * (nfft / 2 + 1) * esz));
     return run_schedule(s, in, out);
 }
 
@@ -191,6 +247,10 @@ int emu_c2r(int dtype, int nfft, int lmax, const void* in, void* out, long long 
     p.bind(p.blob.data());
     Schedule s;
     if (!schedule_c2r(p, batch, nfft / 2 + 1, nfft, s)) return -3;
+    const long long esz = cpx_size(dtype);
+    EmuOwn own_p(p.blob.data(), p.blob.size());
+    EmuOwn own_i(in, (size_t)(batch * (nfft / 2 + 1) * esz));
+    EmuOwn own_o(out, (size_t)(batch * nfft * esz / 2));
     return run_schedule(s, in, out);
 }
 
@@ -201,6 +261,10 @@ int emu_axis(int dtype, const int* dims, int ndims, int axis, int inverse, void*
     p.bind(p.blob.data());
     Schedule s;
     if (!schedule_axis(p, dims, ndims, axis, 1, 0, 1, s)) return -3;
+    long long total = 1;
+    for (int i = 0; i < ndims; ++i) total *= dims[i];
+    EmuOwn own_p(p.blob.data(), p.blob.size());
+    EmuOwn own_b(buf, (size_t)(total * cpx_size(dtype)));
     return run_schedule(s, buf, buf);
 }
 
@@ -214,6 +278,10 @@ int emu_fastfir(const float* H, long long nfft, long long L, const float* x, lon
     iv.bind(iv.blob.data());
     Schedule s;
     if (!schedule_fastfir(fw, iv, L, Ns, 0, s)) return -3;
+    EmuOwn own_f(fw.blob.data(), fw.blob.size()), own_v(iv.blob.data(), iv.blob.size());
+    EmuOwn own_h(H, (size_t)(nfft / 2 + 1) * 2 * sizeof(float));
+    EmuOwn own_x(x, (size_t)Ns * sizeof(float));
+    EmuOwn own_y(y, (size_t)(Ns >= L ? Ns - L + 1 : 0) * sizeof(float));
     return run_schedule(s, x, y, H);
 }
 

@@ -37,6 +37,17 @@ def emu():
     return ctypes.CDLL(EMU)
 
 
+@pytest.fixture(autouse=True)
+def in_bounds(emu):
+    """Every test: no shared-tile, global or table access of the engine fell
+    outside the memory its run owns (KF_MEM_CHECK hooks, counted by the
+    emulator)."""
+    emu.emu_oob_take.restype = ctypes.c_longlong
+    emu.emu_oob_take()
+    yield
+    assert emu.emu_oob_take() == 0, "out-of-bounds accesses"
+
+
 def p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
@@ -273,3 +284,20 @@ def test_overflow_counts_match_reference(emu):
         finally:
             emu.emu_force_col(0)
     assert ran > 2 * len(cases)
+
+
+def test_bounds_check_catches_short_regions(emu):
+    """The bounds check fires: with the output region or the shared tile
+    declared 8 bytes short of the real buffers (which keep their full size),
+    the engine's last accesses are counted as out of bounds."""
+    x = inputs.cpx((2, 480), "int16_t", 1)
+    y = np.zeros_like(x)
+    for which in (1, 2):
+        emu.emu_trim(which, L(8))
+        try:
+            assert emu.emu_c2c(DT["int16_t"], 480, 0, 0, p(x), p(y), L(2), L(480), L(1), L(480)) == 0
+        finally:
+            emu.emu_trim(which, L(0))
+        assert emu.emu_oob_take() > 0, which
+    assert emu.emu_c2c(DT["int16_t"], 480, 0, 0, p(x), p(y), L(2), L(480), L(1), L(480)) == 0
+    assert np.array_equal(y, kfo.fft(x, 0, "int16_t"))
