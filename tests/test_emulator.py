@@ -301,3 +301,26 @@ def test_bounds_check_catches_short_regions(emu):
         assert emu.emu_oob_take() > 0, which
     assert emu.emu_c2c(DT["int16_t"], 480, 0, 0, p(x), p(y), L(2), L(480), L(1), L(480)) == 0
     assert np.array_equal(y, kfo.fft(x, 0, "int16_t"))
+
+
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t"])
+def test_every_small_size(emu, dtype):
+    """Exhaustive small sizes: every complex nfft 1..1100 in both directions
+    (every generic prime up to 1097 included) and every even real nfft
+    2..1100 forward and inverse, bit for bit against the oracle (and in
+    bounds, as every emulator test)."""
+    for n in range(1, 1101):
+        for inv in (0, 1):
+            x = inputs.cpx((3, n), dtype, 7 * n + inv)
+            y = np.zeros_like(x)
+            assert emu.emu_c2c(DT[dtype], n, inv, 0, p(x), p(y), L(3), L(n), L(1), L(n)) == 0, n
+            assert np.array_equal(y, kfo.fft(x, inv, dtype)), (n, inv)
+    for nfft in range(2, 1101, 2):
+        t = inputs.real((3, nfft), dtype, nfft)
+        f = kfo.empty_cpx((3, nfft // 2 + 1), dtype)
+        assert emu.emu_r2c(DT[dtype], nfft, 0, p(t), p(f), L(3)) == 0, nfft
+        assert np.array_equal(f, kfo.fftr(t, dtype)), nfft
+        g = inputs.cpx((3, nfft // 2 + 1), dtype, nfft + 1)
+        t2 = np.zeros((3, nfft), kfo.SCALAR[dtype])
+        assert emu.emu_c2r(DT[dtype], nfft, 0, p(g), p(t2), L(3)) == 0, nfft
+        assert np.array_equal(t2, kfo.fftri(g, nfft, dtype)), nfft
