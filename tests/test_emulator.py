@@ -121,7 +121,8 @@ def test_real(emu, dtype):
 
 @pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
 def test_nd_axes(emu, dtype):
-    for dims in [[2, 3], [4, 4], [3, 5, 7], [8, 6], [2, 3, 4, 6], [64, 64], [5, 7, 11]]:
+    for dims in [[2, 3], [4, 4], [3, 5, 7], [8, 6], [2, 3, 4, 6], [64, 64], [5, 7, 11], [1024, 3], [3, 1024],
+                 [17, 19, 23], [1, 480], [37, 2]]:
         for inv in (0, 1):
             x = inputs.cpx(tuple(dims), dtype, 11)
             buf = x.copy()
@@ -137,7 +138,8 @@ def test_nd_axes(emu, dtype):
 
 def test_fastfir(emu):
     rng = np.random.default_rng(4)
-    for Lh, Ns in [(255, 20000), (1000, 50000), (17, 5000), (255, 2301), (255, 254)]:
+    for Lh, Ns in [(255, 20000), (1000, 50000), (17, 5000), (255, 2301), (255, 254), (2, 3000), (4095, 30000),
+                   (4095, 4095), (1, 100)]:
         h = rng.standard_normal(Lh).astype(np.float32)
         x = rng.standard_normal(Ns).astype(np.float32)
         nfft = kfo.fastfir_nfft(Lh)
