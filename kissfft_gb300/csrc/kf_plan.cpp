@@ -367,6 +367,27 @@ static void finish(Step& st, const LaunchCfg& c) {
     st.args.ntiles = c.grid;
 }
 
+// The kernels index one transform's elements as (local offset) * stride in
+// 32-bit arithmetic (per-transform bases are 64-bit).  A schedule whose
+// strides would leave that range (huge N-D arrays, huge kiss_fft_stride
+// strides) is refused here, on the host, instead of addressing wrong memory.
+static bool fits(Schedule& s) {
+    const long long lim = 0x7fffffffLL;
+    for (const Step& st : s.steps) {
+        if (st.kind != 0) continue;
+        const KArgs& a = st.args;
+        long long L = a.sub[0].L;
+        if (a.nsub > 1) L = std::max<long long>(L, a.sub[1].L);
+        const long long stride = std::max(a.in_stride, a.out_stride);
+        if (stride > lim || (L - 1) * stride > lim) {
+            s.error = "element strides of this call exceed the kernels' 32-bit in-transform offsets";
+            s.steps.clear();
+            return false;
+        }
+    }
+    return true;
+}
+
 bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long in_stride, long long out_dist,
                   Schedule& s) {
     s.steps.clear();
@@ -386,7 +407,7 @@ bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long i
         st.args.out_stride = 1;
         finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2C, batch, 0, 0));
         s.steps.push_back(st);
-        return true;
+        return fits(s);
     }
     const long long Ps = p.sub[1].L, LA = p.sub[0].L, n = p.n;
     Step a;
@@ -425,7 +446,7 @@ bool schedule_c2c(const Plan& p, long long batch, long long in_dist, long long i
     s.steps.push_back(a);
     s.steps.push_back(b);
     s.scratch[0] = (size_t)batch * n * esz;
-    return true;
+    return fits(s);
 }
 
 // Real split / merge as separate elementwise launches (two-pass real plans).
@@ -475,7 +496,7 @@ bool schedule_r2c(const Plan& p, long long batch, long long in_dist, long long o
         st.out_role = out_role;
         finish(st, default_cfg(p.sub[0], p.dtype, MODE_R2C, batch, 0, 0));
         s.steps.push_back(st);
-        return true;
+        return fits(s);
     }
     Schedule c;
     schedule_c2c(p, batch, in_dist / 2, 1, p.n, c);
@@ -485,7 +506,7 @@ bool schedule_r2c(const Plan& p, long long batch, long long in_dist, long long o
     s.steps.push_back(elementwise(1, p, batch, p.n, out_dist, 3, out_role));
     s.scratch[0] = c.scratch[0];
     s.scratch[1] = (size_t)batch * p.n * esz;
-    return true;
+    return fits(s);
 }
 
 bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long out_dist, Schedule& s, int in_role,
@@ -513,7 +534,7 @@ bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long o
         st.out_role = out_role;
         finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2R, batch, 0, 0));
         s.steps.push_back(st);
-        return true;
+        return fits(s);
     }
     s.steps.push_back(elementwise(2, p, batch, in_dist, p.n, in_role, 3));
     Schedule c;
@@ -523,7 +544,7 @@ bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long o
     for (auto& st : c.steps) s.steps.push_back(st);
     s.scratch[0] = c.scratch[0];
     s.scratch[1] = (size_t)batch * p.n * esz;
-    return true;
+    return fits(s);
 }
 
 bool schedule_axis(const Plan& p, const int* dims, int ndims, int axis, long long batch, int in_role, int out_role,
@@ -565,7 +586,7 @@ bool schedule_axis(const Plan& p, const int* dims, int ndims, int axis, long lon
         finish(st, default_cfg(p.sub[0], p.dtype, MODE_C2C, st.args.G, 1, 1));
     }
     s.steps.push_back(st);
-    return true;
+    return fits(s);
 }
 
 bool schedule_fastfir(const Plan& fw, const Plan& iv, long long L, long long Ns, long long, Schedule& s) {
@@ -604,7 +625,7 @@ bool schedule_fastfir(const Plan& fw, const Plan& iv, long long L, long long Ns,
     st.args.fir_ngood = (int)ngood;
     finish(st, default_cfg(fw.sub[0], fw.dtype, MODE_FIR, st.args.G, 0, 0));
     if (st.args.G > 0) s.steps.push_back(st);
-    return true;
+    return fits(s);
 }
 
 }  // namespace kf

@@ -326,3 +326,19 @@ def test_every_small_size(emu, dtype):
         t2 = np.zeros((3, nfft), kfo.SCALAR[dtype])
         assert emu.emu_c2r(DT[dtype], nfft, 0, p(g), p(t2), L(3)) == 0, nfft
         assert np.array_equal(t2, kfo.fftri(g, nfft, dtype)), nfft
+
+
+def test_refuses_offsets_beyond_32_bits(emu):
+    """Strides whose in-transform offsets would pass 2^31 - 1 elements (a
+    huge kiss_fft_stride stride, an N-D axis over 2^30 other elements) are
+    refused when the schedule is built, before any memory is touched (the
+    buffers passed here are tiny and never read)."""
+    x = np.zeros((1, 2), np.int16)
+    y = np.zeros((1, 2), np.int16)
+    st = 3_000_000  # 999 * 3e6 > 2^31
+    assert emu.emu_c2c(DT["int16_t"], 1000, 0, 0, p(x), p(y), L(1), L(1000 * st), L(st), L(1000)) == -3
+    st = 2_150_000  # just over: 999 * 2.15e6 > 2^31 - 1 (2_149_634 is the first stride that does not fit)
+    assert emu.emu_c2c(DT["int16_t"], 1000, 0, 0, p(x), p(y), L(1), L(1000 * st), L(st), L(1000)) == -3
+    dims = (ctypes.c_int * 2)(3, 1 << 30)
+    assert emu.emu_axis(DT["float"], dims, 2, 0, 0, p(x)) == -3
+
