@@ -144,7 +144,7 @@ def main():
             try:
                 f = ref.fftndr(t, dims, dt)
             except MemoryError:
-                # kiss_fftndr_alloc's size heuristic (kiss_fftndr.c:238-247)
+                # kiss_fftndr_alloc's size heuristic (kiss_fftndr.c:50-59)
                 # rejects some small fixed-point shapes; record that.
                 gold["ndr"].append({"dtype": dt, "dims": dims, "seed": seed, "ref_rejects": True})
                 continue
