@@ -96,3 +96,25 @@ def test_bench_accuracy_helpers():
         rows.append({"accuracy": a})
     s = bench.accuracy_summary(rows)
     assert s["fixed_bit_exact"] and s["float_within_bound"] and s["rows_per_unit"] == 3
+
+
+def test_bench_reference_arm_line():
+    """bench.py --impl reference (CPU only) prints one JSON line with the
+    keys the benchmark contract names, on a tiny sample of the workload."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3", "--cpu-frac", "0.002"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["warmup"] >= 3 and line["value"] > 0
+    cb = line["cpu_baseline"]
+    for k in ("value", "unit", "cores", "kind", "sample"):
+        assert k in cb, k
+    assert cb["openmp_build"]["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert "workload" in line["config"]
