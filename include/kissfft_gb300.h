@@ -76,11 +76,15 @@ int kfg_exec_batch(kfg_plan *p, const void *in, void *out, long long batch, long
  * reference, whose transforms run on the host.  Complex 1-D plans and device
  * pointers only.  Scratch of two-pass plans (batch * nfft complex elements)
  * comes from one fixed device array per device of KFG_NOALLOC_SCRATCH_BYTES;
- * a larger batch fails with KFG_EINVAL.  Calls that may overlap on the GPU
- * (other streams or threads) race on that array: issue them on one stream.
- * The first call on a device looks the array up (and may load the module
- * holding it): make it before any stream capture.  Run-time specialised
- * kernels are not used. */
+ * a larger batch fails with KFG_EINVAL.  The stream and both buffers must be
+ * on the current device (the array used is the current device's); a stream
+ * or buffer of another device fails with KFG_EINVAL.  Calls that may overlap
+ * on the GPU (other streams or threads) race on that array: issue them on
+ * one stream.  The first call in a context looks the array up (and may load
+ * the module holding it, which reserves the array's bytes): make it before
+ * any stream capture.  The address is kept per context, so calls after a
+ * device reset look it up again.  Run-time specialised kernels are not
+ * used. */
 #define KFG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
 int kfg_exec_batch_noalloc(kfg_plan *p, const void *in, void *out, long long batch, long long in_dist,
                            long long out_dist, void *stream);
@@ -239,6 +243,15 @@ int kfg_server_loadtest(kfg_server *s, const kfg_loadtest *cfg, kfg_loadtest_res
  * dtype, out[2] = length, out[3] = number of HBM passes of a 1-D plan,
  * out[4] = kernel family, out[5] = tile length. */
 int kfg_plan_info(const kfg_plan *p, int *out, int nout);
+/* Reads a table back from a plan's device memory (the bytes the kernels
+ * use), for tests that compare it with the reference's: which = 0, the full
+ * twiddle table of a complex plan (nfft entries of the sample type,
+ * kiss_fft.c:361-367; for a real plan, that of its nfft/2-point complex
+ * sub-transform), which = 1, the super twiddles of a real plan (nfft/4
+ * entries, kiss_fftr.c:53-59).  Returns the table's byte count and copies
+ * min(bytes, count) bytes to host when host != NULL; a negative KFG_E*
+ * code on error. */
+long long kfg_plan_table(const kfg_plan *p, int which, void *host, size_t bytes);
 
 #ifdef __cplusplus
 }

@@ -71,6 +71,8 @@ def core():
         L.kfg_get_stream.restype = vp
         L.kfg_last_error.restype = ctypes.c_char_p
         L.kfg_plan_info.argtypes = [vp, vp, i]
+        L.kfg_plan_table.restype = ll
+        L.kfg_plan_table.argtypes = [vp, i, vp, ctypes.c_size_t]
         _core = L
     return _core
 

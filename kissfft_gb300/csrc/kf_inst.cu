@@ -62,11 +62,12 @@ cudaError_t KF_ENGINE_M(KF_INST_MODE)(const Step& st, cudaStream_t s) {
 cudaError_t KF_MULTI_M(KF_INST_MODE)(const MultiArgs& m, int T, int smem, long long grid, cudaStream_t s) {
     constexpr kmask_t KM = family_mask(KF_INST_FAM, KF_INST_DT == 0);
     const void* k = (const void*)kf_multi_kernel<kf_inst_s, KF_INST_MODE, KM>;
-    static bool attr_done = false;
-    if (!attr_done) {
+    static std::atomic<unsigned long long> attr_ctx{0};
+    const unsigned long long ctx = current_context_id();
+    if (ctx == 0 || attr_ctx.load() != ctx) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess) return e;
-        attr_done = true;
+        attr_ctx.store(current_context_id());
     }
     if (grid <= 0) {
         int per = 0, nsm = 0, dev = 0;

@@ -6,9 +6,17 @@
 #include "kf_device.cuh"
 #include "kf_plan.h"
 
+#include <atomic>
 #include <string>
 
 namespace kf {
+
+// Identity of the calling thread's current CUDA context (cuCtxGetId; 0 when
+// the thread has none).  State that belongs to a context -- kernel
+// attributes, the address of a __device__ array -- is cached per context
+// and set up again when the id changes (after cudaDeviceReset or a reset
+// of the primary context the runtime creates a new context with a new id).
+unsigned long long current_context_id();
 
 // Grid of a launch: one CTA per tile, or -- for TMA-staged steps, which
 // loop over tiles -- as many CTAs as fit on the GPU at once.
@@ -46,11 +54,12 @@ inline long long launch_grid(const void* k, const Step& st) {
 template <typename S, int MODE, int FAM>
 static cudaError_t launch_engine_f(const Step& st, cudaStream_t s) {
     auto k = kf_engine_kernel<S, MODE, FAM>;
-    static bool attr_done = false;
-    if (!attr_done) {
+    static std::atomic<unsigned long long> attr_ctx{0};
+    const unsigned long long ctx = current_context_id();
+    if (ctx == 0 || attr_ctx.load() != ctx) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess) return e;
-        attr_done = true;
+        attr_ctx.store(current_context_id());
     }
     const long long grid = launch_grid((const void*)k, st);
     if (grid <= 0) return cudaSuccess;

@@ -30,6 +30,38 @@
 
 using namespace kf;
 
+namespace kf {
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points, so
+// that the library needs no link to the driver library itself.
+unsigned long long current_context_id() {
+    typedef int (*get_current_t)(void**);
+    typedef int (*get_id_t)(void*, unsigned long long*);
+    static get_current_t get_current = nullptr;
+    static get_id_t get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (get_current_t)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (get_id_t)f;
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    if (get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+}  // namespace kf
+
 namespace {
 
 thread_local std::string g_err;
@@ -1053,6 +1085,28 @@ int kfg_plan_info(const kfg_plan* p, int* out, int nout) {
     }
     for (int i = 0; i < nout && i < 6; ++i) out[i] = v[i];
     return KFG_OK;
+}
+
+long long kfg_plan_table(const kfg_plan* p, int which, void* host, size_t bytes) {
+    if (!p || !p->main || (p->kind != K_C2C && p->kind != K_REAL) || which < 0 || which > 1)
+        return fail(KFG_EINVAL, "kfg_plan_table: needs a complex or real 1-D plan and table 0 or 1");
+    const DevPlan& d = *p->main;
+    const size_t esz = (size_t)esz_of(p->dtype);
+    size_t off = 0, count = 0;
+    if (which == 0) {
+        off = d.p.off_tw_full;
+        count = (size_t)d.p.n * esz;
+    } else {
+        if (d.p.real_nfft <= 0) return fail(KFG_EINVAL, "kfg_plan_table: super twiddles belong to real plans");
+        off = d.p.off_super;
+        count = (size_t)(d.p.n / 2) * esz;
+    }
+    if (host && bytes) {
+        const size_t nb = bytes < count ? bytes : count;
+        cudaError_t e = cudaMemcpy(host, (const char*)d.d + off, nb, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("cudaMemcpy(plan table): ") + cudaGetErrorString(e));
+    }
+    return (long long)count;
 }
 
 }  // extern "C"

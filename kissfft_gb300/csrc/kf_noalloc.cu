@@ -24,10 +24,22 @@
 //    and give wrong results: issue them on one stream.  Nothing in it has to
 //    start at zero: the first pass writes every element the second pass
 //    reads;
-//  - the first call on a device (with the call's stream on the current
-//    device) looks up the array's device address with cudaGetSymbolAddress,
-//    which loads this module if it is not loaded yet.  Make that first call
-//    before any stream capture on that device;
+//  - the stream and both buffers must belong to the current device: the
+//    array used is the current device's.  A stream or buffer of another
+//    device is refused with KFG_EINVAL;
+//  - the first call in a CUDA context of a device (with that device
+//    current) looks up the array's device address with cudaGetSymbolAddress,
+//    which loads this module into the context if it is not loaded yet.  Make
+//    that first call before any stream capture on that device.  The address
+//    is kept per context: after cudaDeviceReset (or a reset of the primary
+//    context) the next call finds a new context and looks the address up
+//    again;
+//  - the array lives in this file's own device module, which holds no
+//    kernel.  With lazy module loading (the CUDA default) that module, and
+//    its 64 MiB, is loaded by the first call of this entry point in a
+//    context; with eager loading (CUDA_MODULE_LOADING=EAGER) every context
+//    of a process that loads this library reserves the 64 MiB, whether it
+//    calls the entry point or not;
 //  - run-time specialised kernels are not used here (their first use
 //    compiles and loads a module), so the precompiled kernels run whatever
 //    kfg_set_specialize says.
@@ -52,24 +64,40 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
-void* g_scratch[kMaxDevices];  // device address of kf_noalloc_scratch, per device, set once
+// device address of kf_noalloc_scratch per device, and the context it was
+// looked up in
+struct ScratchAddr {
+    unsigned long long ctx = 0;
+    void* ptr = nullptr;
+};
+ScratchAddr g_scratch[kMaxDevices];
 
-// Set-up, once per device, with that device current.
-int scratch_of_current_device(void** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+// Set-up, once per device and context, with that device current.
+int scratch_of_current_device(int dev, void** out) {
     if (dev < 0 || dev >= kMaxDevices) return set_error(KFG_EUNSUPPORTED, "kfg_exec_batch_noalloc: device index too large");
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch[dev]) {
+    const unsigned long long ctx = current_context_id();
+    ScratchAddr& a = g_scratch[dev];
+    if (!a.ptr || ctx == 0 || a.ctx != ctx) {
         void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, kf_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&ptr, kf_noalloc_scratch);
         if (e != cudaSuccess || !ptr)
             return set_error(KFG_ECUDA, std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e));
-        g_scratch[dev] = ptr;
+        a.ptr = ptr;
+        a.ctx = current_context_id();  // the lookup makes the device's primary context current if none was
     }
-    *out = g_scratch[dev];
+    *out = a.ptr;
     return KFG_OK;
+}
+
+// The device a pointer's memory belongs to, or -1.
+int device_of(const void* ptr) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return a.device;
 }
 
 // launch_step without the run-time specialised kernels
@@ -101,6 +129,15 @@ extern "C" int kfg_exec_batch_noalloc(kfg_plan* p, const void* in, void* out, lo
     Schedule s;
     int rc = c2c_schedule(p, batch, in_dist, out_dist, s);
     if (rc) return rc;
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    const cudaStream_t st = stream_or_default(stream);
+    int sdev = -1;
+    e = cudaStreamGetDevice(st, &sdev);
+    if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("cudaStreamGetDevice: ") + cudaGetErrorString(e));
+    if (sdev != dev || device_of(in) != dev || device_of(out) != dev)
+        return set_error(KFG_EINVAL, "kfg_exec_batch_noalloc: the stream and both buffers must be on the current device");
     const size_t off1 = (s.scratch[0] + 255) & ~(size_t)255;
     const size_t need = s.scratch[1] ? off1 + s.scratch[1] : s.scratch[0];
     if (need > KFG_NOALLOC_SCRATCH_BYTES)
@@ -110,17 +147,16 @@ extern "C" int kfg_exec_batch_noalloc(kfg_plan* p, const void* in, void* out, lo
                                          "; split it into smaller batches");
     void* scratch = nullptr;
     if (need > 0) {
-        rc = scratch_of_current_device(&scratch);
+        rc = scratch_of_current_device(dev, &scratch);
         if (rc) return rc;
     }
-    const cudaStream_t st = stream_or_default(stream);
     void* roles[4] = {(void*)in, out, scratch, scratch ? (char*)scratch + off1 : nullptr};
     for (auto& step : s.steps) {
         step.args.in = roles[step.in_role];
         step.args.out = roles[step.out_role];
         step.args.fir_H = nullptr;
         enable_tma(step, step.args.in);
-        cudaError_t e = launch_precompiled(step, st);
+        e = launch_precompiled(step, st);
         if (e != cudaSuccess) return set_error(KFG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     }
     return KFG_OK;

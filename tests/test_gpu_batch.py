@@ -1,12 +1,16 @@
 """The batched uneven-mix API (kfg_batch_*) through the C ABI.
 
-Every request of a mix must give the same result in the batch -- run
-directly, replayed from a CUDA graph, and in the per-call form -- as when it
-runs alone through kfg_exec_batch: Q15 bit for bit, float within
-2e-7*log2(N) relative L2.  Float complex requests are also checked against
-an FP64 DFT.  The mixes cover single- and two-pass complex and real plans,
-the real inverse, generic radices and Q15, at arena offsets that are not
-packed.
+Every request of a mix, in every form (run directly, replayed from a CUDA
+graph, and the per-call form), is checked against the oracle -- the C
+restatement of the reference path -- on its own input: Q15 complex
+requests bit for bit against kiss_fft (kiss_fft.c:375-404), float complex
+against kiss_fft and an FP64 DFT, float real forward against kiss_fftr
+(kiss_fftr.c:63-117) and np.fft.rfft, float real inverse against
+kiss_fftri (kiss_fftr.c:119-155) and n * np.fft.irfft, float within
+2e-7*log2(N) relative L2.  Each request must also give the same result in
+the batch as alone through kfg_exec_batch.  The mixes cover single- and
+two-pass complex and real plans, the real inverse, generic radices and
+Q15, at arena offsets that are not packed.
 """
 import ctypes
 
@@ -14,6 +18,7 @@ import numpy as np
 import pytest
 
 import inputs
+from oracle import kfo
 
 pytestmark = pytest.mark.gpu
 
@@ -65,6 +70,22 @@ def request_input(kind, dt, n, seed):
     return np.ascontiguousarray(a).view(np.uint8).ravel()
 
 
+def oracle_result(kind, dt, n, raw):
+    """The oracle's result(s) for one request's input bytes: the bit pattern
+    (uint8) for Q15, else the oracle's float result and an FP64 transform."""
+    if dt == 2:
+        x = raw.view(np.int16).reshape(n, 2)
+        return [np.ascontiguousarray(kfo.fft(x, 0, "int16_t")).view(np.uint8).ravel()]
+    if kind == 1:
+        x = raw.view(np.complex64)
+        return [kfo.fft(x, 0, "float").astype(np.complex128), np.fft.fft(x.astype(np.complex128))]
+    if kind == 2:
+        t = raw.view(np.float32)
+        return [kfo.fftr(t, "float").astype(np.complex128), np.fft.rfft(t.astype(np.float64))]
+    f = raw.view(np.complex64)
+    return [kfo.fftri(f, n, "float").astype(np.float64), n * np.fft.irfft(f.astype(np.complex128), n)]
+
+
 def run_mix(L, mix, target_threads=256):
     import torch
     reqs, ib_tot, ob_tot = layout(mix, gap=64)
@@ -105,20 +126,22 @@ def run_mix(L, mix, target_threads=256):
         results["percall"] = outd.cpu().numpy()
     finally:
         L.kfg_batch_free(B)
+    oracle = [oracle_result(kind, dt, n, host[io:io + ib]) for (kind, dt, n, io, oo, ib, ob) in reqs]
     for form, got in results.items():
         for k, (kind, dt, n, io, oo, ib, ob) in enumerate(reqs):
             g, a = got[oo:oo + ob], alone_h[oo:oo + ob]
             if dt == 2:
                 assert np.array_equal(g, a), (form, k, kind, n)
+                assert np.array_equal(g, oracle[k][0]), ("oracle", form, k, kind, n)
             else:
                 gv, av = g.view(np.float32), a.view(np.float32)
+                tol = 2e-7 * max(1.0, np.log2(n))
                 err = np.linalg.norm(gv - av) / max(np.linalg.norm(av), 1e-30)
-                assert err <= 2e-7 * max(1.0, np.log2(n)), (form, k, kind, n, err)
-                if kind == 1:
-                    x = host[io:io + ib].view(np.complex64).astype(np.complex128)
-                    ex = np.fft.fft(x)
-                    e2 = np.linalg.norm(gv.view(np.complex64) - ex) / np.linalg.norm(ex)
-                    assert e2 <= 2e-7 * max(1.0, np.log2(n)), (form, k, n, e2)
+                assert err <= tol, (form, k, kind, n, err)
+                gc = gv.view(np.complex64) if kind != 3 else gv
+                for ref in oracle[k]:
+                    e2 = np.linalg.norm(gc.astype(ref.dtype) - ref) / max(np.linalg.norm(ref), 1e-30)
+                    assert e2 <= tol, ("oracle", form, k, kind, n, e2)
     return results
 
 

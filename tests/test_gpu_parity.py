@@ -56,6 +56,29 @@ def test_c2c_golden(kf, golden, dtype):
         cfg.free()
 
 
+def test_device_plan_tables_match_the_reference(kf, golden):
+    """The twiddle tables the kernels read, copied back from the device plan,
+    hash-match the reference's cfg->twiddles (kiss_fft.c:361-367) and the
+    real plans' super twiddles (kiss_fftr.c:53-59), for all four sample
+    types and both directions."""
+    import ctypes
+    L = kf.core()
+    code = {"float": 0, "double": 1, "int16_t": 2, "int32_t": 3}
+    for key, make, which, nkey in (("twiddles", L.kfg_plan_c2c, 0, "n"),
+                                   ("super_twiddles", L.kfg_plan_real, 1, "nfft")):
+        for c in golden[key]:
+            p = make(code[c["dtype"]], c[nkey], c["inverse"])
+            assert p, (c, L.kfg_last_error())
+            try:
+                nb = L.kfg_plan_table(p, which, None, 0)
+                assert nb > 0, (c, L.kfg_last_error())
+                buf = (ctypes.c_uint8 * nb)()
+                assert L.kfg_plan_table(p, which, buf, nb) == nb
+                assert sha(np.frombuffer(buf, np.uint8)) == c["sha256"], c
+            finally:
+                L.kfg_plan_free(p)
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_c2c_host_pointers_single_calls(kf, dtype):
     """kiss_fft with host buffers, one transform per call (the reference's own

@@ -2,11 +2,17 @@
 
 Requests of every kind (c2c float and Q15, real forward and inverse, 2-D,
 fast FIR), with device, pinned-host and ordinary host buffers, are submitted
-from several threads at once.  Each result must equal the same request run
-alone through the plain API: Q15 bit for bit, float within 2e-7*log2(N)
-relative L2 (2-D: N = rows*cols; fast FIR: 1e-6 relative).  A budget smaller
-than the mix forces requests to queue for admission; a request larger than
-the whole budget fails on its own without disturbing the others.
+from several threads at once.  Each served result is checked against the
+oracle (the C restatement of the reference path) on its own input --
+kiss_fft (kiss_fft.c:375-404) with Q15 bit for bit, kiss_fftr / kiss_fftri
+(kiss_fftr.c:63-155), kiss_fftnd (kiss_fftnd.c:156-188), and for the fast
+FIR np.convolve within 4x the error of the reference's own overlap-scrap
+filter (tools/kiss_fastfir.c:167-239) -- float within 2e-7*log2(N) relative
+L2 (2-D: N = rows*cols).  It must also equal the same request run alone
+through the plain API (the same tolerances; fast FIR 1e-6 relative).  A
+budget smaller than the mix forces requests to queue for admission; a
+request larger than the whole budget fails on its own without disturbing
+the others.
 """
 import threading
 
@@ -14,6 +20,7 @@ import numpy as np
 import pytest
 
 import inputs
+from oracle import kfo
 
 pytestmark = pytest.mark.gpu
 
@@ -121,6 +128,35 @@ def close(kind, dt, n, got, ref):
     return np.linalg.norm(g - r) <= tol * max(np.linalg.norm(r), 1e-30)
 
 
+def relerr(got, ref):
+    g = np.asarray(got).astype(np.complex128 if np.iscomplexobj(got) or np.iscomplexobj(ref) else np.float64)
+    r = np.asarray(ref).astype(g.dtype)
+    return float(np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-30))
+
+
+def oracle_ok(kind, dt, n, x, got):
+    """The served result against the oracle on the same input."""
+    if kind == "fir":
+        h, ns = n
+        exact = np.convolve(x.astype(np.float64), h.astype(np.float64), "valid")
+        ref_err = relerr(kfo.fastfir(h, x), exact)  # the reference's own overlap-scrap error
+        return relerr(got, exact) <= max(4 * ref_err, 1e-6)
+    if kind == "c2c":
+        ref = kfo.fft(x, 0, dt)
+        if dt == "int16_t":
+            return np.array_equal(got, ref)
+        exact = np.fft.fft(x.astype(np.complex128))
+    elif kind == "r2c":
+        ref, exact = kfo.fftr(x, dt), np.fft.rfft(x.astype(np.float64))
+    elif kind == "c2r":
+        ref, exact = kfo.fftri(x, n, dt), n * np.fft.irfft(x.astype(np.complex128), n)
+    else:
+        ref, exact = kfo.fftnd(x, list(n), 0, dt), np.fft.fft2(x.astype(np.complex128))
+    N = n[0] * n[1] if kind == "2d" else n
+    tol = 2e-7 * max(1.0, np.log2(N))
+    return relerr(got, ref) <= tol and relerr(got, exact) <= tol
+
+
 def test_mix_from_threads_matches_alone(kf):
     import torch
     reqs = make_requests(kf, 40)
@@ -162,6 +198,7 @@ def test_mix_from_threads_matches_alone(kf):
                 torch.cuda.synchronize()
                 y = y.cpu().numpy().view(refs[i].dtype).reshape(refs[i].shape)
             assert close(kind, dt, n, y, refs[i]), (i, kind, dt, n)
+            assert oracle_ok(kind, dt, n, x, y), ("oracle", i, kind, dt, n)
         st = srv.stats()
         assert st["completed"] == len(reqs) and st["failed"] == 0
         assert 0 < st["p50_s"] <= st["p99_s"] <= st["max_s"]
@@ -188,6 +225,8 @@ def test_admission_under_a_small_budget(kf):
             assert srv.wait(rid, timeout=60.0) is not None
         ref = alone(kf, "c2c", "float", n, xs[5])
         assert close("c2c", "float", n, ys[5], ref)
+        for k in range(0, 64, 9):
+            assert oracle_ok("c2c", "float", n, xs[k], ys[k]), k
         st = srv.stats()
         assert st["completed"] == 64 and st["failed"] == 1
         assert st["peak_hbm_bytes"] <= 4 << 20
@@ -216,6 +255,7 @@ def test_plan_cache_evicts_under_the_budget(kf):
         for k in (0, 13, 29):
             n = sizes[k % len(sizes)]
             assert close("c2c", "float", n, ys[k], alone(kf, "c2c", "float", n, xs[k]))
+            assert oracle_ok("c2c", "float", n, xs[k], ys[k]), k
         st = srv.stats()
         assert st["completed"] == 30 and st["failed"] == 0
         assert st["evictions"] > 0
