@@ -80,6 +80,16 @@ struct ArIeee {
         c.i *= s;
         return c;
     }
+    // "wide" forms (see ArFixed): for IEEE types they are the plain ones
+    typedef cpx<S> CW;
+    static KF_HD CW widen(C c) { return c; }
+    static KF_HD C narrow(CW c) { return c; }
+    static KF_HD W tr(W x) { return x; }
+    template <int P>
+    static KF_HD CW fixdiv_w(CW c) { return c; }
+    static KF_HD CW cmul_w(CW a, C b) { return cmul(a, b); }
+    static KF_HD W smul_w(W a, S b) { return a * b; }
+    static KF_HD CW mulsc_w(CW c, S s) { return mulsc(c, s); }
 };
 
 template <typename S, typename P, int FB, int64_t SMAX>
@@ -163,6 +173,113 @@ struct ArFixed {
         c.i = st(round1(c.i, s));
         return c;
     }
+    // "Wide" forms for the butterflies.  The reference stores every sum in a
+    // sample (truncation to the storage width), but truncation commutes with
+    // the wrapping adds and subtracts, so a chain of them may keep its
+    // values untruncated (CW: complex of W) and truncate once where the
+    // stored value feeds a multiply or a shift, and at the butterfly's
+    // outputs.  tr(x) is the value the reference would have stored.
+    typedef cpx<W> CW;
+    static KF_HD CW widen(C c) {
+        CW r;
+        r.r = c.r;
+        r.i = c.i;
+        return r;
+    }
+    static KF_HD C narrow(CW c) {
+        C r;
+        r.r = st(c.r);
+        r.i = st(c.i);
+        return r;
+    }
+    static KF_HD W tr(W x) { return (W)st(x); }
+    // sround(a*b + c*d) and sround(a*b - c*d), untruncated, for a and c
+    // within the sample range and |b|, |d| <= SMAX (|a*b| + |c*d| < 2^31
+    // for Q15, so the int32 expression of the reference is exact; the
+    // compiler fuses the shift into the add that consumes the result)
+    static KF_HD W rnd_add(W a, W b, W c, W d) {
+        if constexpr (sizeof(P) == 4)
+            return (a * b + c * d + (1 << (FB - 1))) >> FB;
+        else
+            return round2((S)a, (S)b, (S)c, (S)d);
+    }
+    static KF_HD W rnd_sub(W a, W b, W c, W d) {
+        if constexpr (sizeof(P) == 4)
+            return (a * b - c * d + (1 << (FB - 1))) >> FB;
+        else
+            return round2((S)a, (S)b, (S)c, (S)(0 - d));
+    }
+    static KF_HD W rnd1(W a, W b) {
+        if constexpr (sizeof(P) == 4)
+            return (a * b + (1 << (FB - 1))) >> FB;
+        else
+            return round1((S)a, (S)b);
+    }
+    // C_FIXDIV of a sample value: |result| <= SMAX/Q < 2^(FB-1), no truncation
+    template <int Q>
+    static KF_HD CW fixdiv_w(CW c) {
+        constexpr W k = (W)(SMAX / Q);
+        CW r;
+        r.r = rnd1(c.r, k);
+        r.i = rnd1(c.i, k);
+        return r;
+    }
+    // C_MUL(m, a, b), a within the sample range, b a table twiddle; the
+    // result is left untruncated
+    static KF_HD CW cmul_w(CW a, C b) {
+        CW m;
+        m.r = rnd_sub(a.r, b.r, a.i, b.i);
+        m.i = rnd_add(a.r, b.i, a.i, b.r);
+        return m;
+    }
+    // S_MUL / C_MULBYSCALAR: |a*b| < 2^(2*FB), so the result fits the sample type
+    static KF_HD W smul_w(W a, S b) { return rnd1(a, b); }
+    static KF_HD CW mulsc_w(CW c, S s) {
+        CW r;
+        r.r = rnd1(c.r, s);
+        r.i = rnd1(c.i, s);
+        return r;
+    }
+    // C_MUL(t, a, w) then C_ADDTO(acc, t) of kf_bfly_generic, a within the
+    // sample range, w a table twiddle held as W; acc untruncated
+    static KF_HD void cmul_acc_w(W& ar, W& ai, CW a, CW w) {
+        const W tr_ = rnd_sub(a.r, w.r, a.i, w.i), ti = rnd_add(a.r, w.i, a.i, w.r);
+        KF_OVF_CHECK(S, st(ar), +, st(tr_));
+        KF_OVF_CHECK(S, st(ai), +, st(ti));
+        ar = add(ar, tr_);
+        ai = add(ai, ti);
+    }
+#if defined(__CUDA_ARCH__)
+    // Q31 output of kf_bfly_generic on the device:
+    //   acc = x0 + sum_{q=1..P-1} C_MUL(x_q, w_q)   (each product rounded).
+    // With the legs doubled (x2r = 2*x.r, x2i = 2*x.i, x2n = -2*x.i; they fit
+    // since |x| <= SMAX/P) and v = a*b + c*d exact,
+    //   acc*2^32 + 2^31 + 2v  (mod 2^64)
+    // is two widening multiply-adds, and its high word is acc + sround(v)
+    // (mod 2^32): the rounding shift and the accumulation cost nothing.
+    template <int P>
+    static __device__ __forceinline__ C gen_out_q31(CW x0, const W* x2r, const W* x2i, const W* x2n, const CW* w) {
+        unsigned ar = (unsigned)x0.r, ai = (unsigned)x0.i;
+#pragma unroll
+        for (int q = 1; q < P; ++q) {
+            unsigned long long cr, ci;
+            unsigned lo;
+            asm("mov.b64 %0, {%1, %2};" : "=l"(cr) : "r"(1u << FB), "r"(ar));
+            asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(cr) : "r"((int)x2r[q]), "r"((int)w[q - 1].r));
+            asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(cr) : "r"((int)x2n[q]), "r"((int)w[q - 1].i));
+            asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(ar) : "l"(cr));
+            asm("mov.b64 %0, {%1, %2};" : "=l"(ci) : "r"(1u << FB), "r"(ai));
+            asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(ci) : "r"((int)x2r[q]), "r"((int)w[q - 1].i));
+            asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(ci) : "r"((int)x2i[q]), "r"((int)w[q - 1].r));
+            asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(ai) : "l"(ci));
+            (void)lo;
+        }
+        C out;
+        out.r = (S)ar;
+        out.i = (S)ai;
+        return out;
+    }
+#endif
     // C_MUL(t, a, w) then C_ADDTO(acc, t) of kf_bfly_generic, with acc kept as
     // an untruncated word: truncation to S commutes with the wrapping adds, so
     // the caller truncates once after the whole sum.  Twiddles have
@@ -208,6 +325,29 @@ KF_HD cpx<S> c_sub(cpx<S> a, cpx<S> b) {
     return r;
 }
 
+// C_ADD / C_SUB on wide values (no truncation; the overflow hook sees the
+// values the reference stored)
+template <typename S>
+KF_HD typename Ar<S>::CW w_add(typename Ar<S>::CW a, typename Ar<S>::CW b) {
+    typedef Ar<S> A;
+    KF_OVF_CHECK(S, A::tr(a.r), +, A::tr(b.r));
+    KF_OVF_CHECK(S, A::tr(a.i), +, A::tr(b.i));
+    typename A::CW r;
+    r.r = A::add(a.r, b.r);
+    r.i = A::add(a.i, b.i);
+    return r;
+}
+template <typename S>
+KF_HD typename Ar<S>::CW w_sub(typename Ar<S>::CW a, typename Ar<S>::CW b) {
+    typedef Ar<S> A;
+    KF_OVF_CHECK(S, A::tr(a.r), -, A::tr(b.r));
+    KF_OVF_CHECK(S, A::tr(a.i), -, A::tr(b.i));
+    typename A::CW r;
+    r.r = A::sub(a.r, b.r);
+    r.i = A::sub(a.i, b.i);
+    return r;
+}
+
 // ---------------------------------------------------------------- butterflies
 // v[0], v[VS], ..., v[(P-1)*VS] are the P legs of one butterfly (register
 // array, compile-time stride).  w[q-1] is the twiddle of leg q.  The
@@ -217,23 +357,25 @@ KF_HD cpx<S> c_sub(cpx<S> a, cpx<S> b) {
 template <typename S, int VS>
 KF_HD void bfly2(cpx<S>* v, const cpx<S>* w) {
     typedef Ar<S> A;
-    cpx<S> a = A::template fixdiv<2>(v[0]), b = A::template fixdiv<2>(v[VS]);
-    cpx<S> t = A::cmul(b, w[0]);
-    v[VS] = c_sub(a, t);
-    v[0] = c_add(a, t);
+    typedef typename A::CW CW;
+    CW a = A::template fixdiv_w<2>(A::widen(v[0])), b = A::template fixdiv_w<2>(A::widen(v[VS]));
+    CW t = A::cmul_w(b, w[0]);
+    v[VS] = A::narrow(w_sub<S>(a, t));
+    v[0] = A::narrow(w_add<S>(a, t));
 }
 
 // kf_bfly4, kiss_fft.c:38-84
 template <typename S, int VS>
 KF_HD void bfly4(cpx<S>* v, const cpx<S>* w, bool inverse) {
     typedef Ar<S> A;
-    cpx<S> a0 = A::template fixdiv<4>(v[0]), a1 = A::template fixdiv<4>(v[VS]);
-    cpx<S> a2 = A::template fixdiv<4>(v[2 * VS]), a3 = A::template fixdiv<4>(v[3 * VS]);
-    cpx<S> t0 = A::cmul(a1, w[0]), t1 = A::cmul(a2, w[1]), t2 = A::cmul(a3, w[2]);
-    cpx<S> d02 = c_sub(a0, t1), s02 = c_add(a0, t1);
-    cpx<S> s13 = c_add(t0, t2), d13 = c_sub(t0, t2);
-    v[2 * VS] = c_sub(s02, s13);
-    v[0] = c_add(s02, s13);
+    typedef typename A::CW CW;
+    CW a0 = A::template fixdiv_w<4>(A::widen(v[0])), a1 = A::template fixdiv_w<4>(A::widen(v[VS]));
+    CW a2 = A::template fixdiv_w<4>(A::widen(v[2 * VS])), a3 = A::template fixdiv_w<4>(A::widen(v[3 * VS]));
+    CW t0 = A::cmul_w(a1, w[0]), t1 = A::cmul_w(a2, w[1]), t2 = A::cmul_w(a3, w[2]);
+    CW d02 = w_sub<S>(a0, t1), s02 = w_add<S>(a0, t1);
+    CW s13 = w_add<S>(t0, t2), d13 = w_sub<S>(t0, t2);
+    v[2 * VS] = A::narrow(w_sub<S>(s02, s13));
+    v[0] = A::narrow(w_add<S>(s02, s13));
     cpx<S> o1, o3;
     if (inverse) {
         o1.r = A::st(A::sub(d02.r, d13.i));
@@ -250,53 +392,63 @@ KF_HD void bfly4(cpx<S>* v, const cpx<S>* w, bool inverse) {
     v[3 * VS] = o3;
 }
 
-// kf_bfly3, kiss_fft.c:86-128 (c0 = epi3 = tw[fstride*m])
+// kf_bfly3, kiss_fft.c:86-128 (c0 = epi3 = tw[fstride*m]).  HALF_OF and
+// C_MULBYSCALAR act on the stored (truncated) sums.
 template <typename S, int VS>
 KF_HD void bfly3(cpx<S>* v, const cpx<S>* w, cpx<S> c0) {
     typedef Ar<S> A;
-    cpx<S> a0 = A::template fixdiv<3>(v[0]), a1 = A::template fixdiv<3>(v[VS]);
-    cpx<S> a2 = A::template fixdiv<3>(v[2 * VS]);
-    cpx<S> t1 = A::cmul(a1, w[0]), t2 = A::cmul(a2, w[1]);
-    cpx<S> s = c_add(t1, t2), d = c_sub(t1, t2);
+    typedef typename A::CW CW;
+    typedef typename A::W W;
+    CW a0 = A::template fixdiv_w<3>(A::widen(v[0])), a1 = A::template fixdiv_w<3>(A::widen(v[VS]));
+    CW a2 = A::template fixdiv_w<3>(A::widen(v[2 * VS]));
+    CW t1 = A::cmul_w(a1, w[0]), t2 = A::cmul_w(a2, w[1]);
+    CW s = w_add<S>(t1, t2), d = w_sub<S>(t1, t2);
+    const W o1r = A::sub(a0.r, A::half(A::tr(s.r))), o1i = A::sub(a0.i, A::half(A::tr(s.i)));
+    CW dt;
+    dt.r = A::tr(d.r);
+    dt.i = A::tr(d.i);
+    const CW dm = A::mulsc_w(dt, c0.i);
+    v[0] = A::narrow(w_add<S>(a0, s));
     cpx<S> o1, o2;
-    o1.r = A::st(A::sub(a0.r, A::half(s.r)));
-    o1.i = A::st(A::sub(a0.i, A::half(s.i)));
-    d = A::mulsc(d, c0.i);
-    v[0] = c_add(a0, s);
-    o2.r = A::st(A::add(o1.r, d.i));
-    o2.i = A::st(A::sub(o1.i, d.r));
-    o1.r = A::st(A::sub(o1.r, d.i));
-    o1.i = A::st(A::add(o1.i, d.r));
+    o2.r = A::st(A::add(o1r, dm.i));
+    o2.i = A::st(A::sub(o1i, dm.r));
+    o1.r = A::st(A::sub(o1r, dm.i));
+    o1.i = A::st(A::add(o1i, dm.r));
     v[VS] = o1;
     v[2 * VS] = o2;
 }
 
-// kf_bfly5, kiss_fft.c:130-189 (c0 = ya = tw[fstride*m], c1 = yb = tw[2*fstride*m])
+// kf_bfly5, kiss_fft.c:130-189 (c0 = ya = tw[fstride*m], c1 = yb = tw[2*fstride*m]).
+// S_MUL acts on the stored (truncated) sums and differences.
 template <typename S, int VS>
 KF_HD void bfly5(cpx<S>* v, const cpx<S>* w, cpx<S> ya, cpx<S> yb) {
     typedef Ar<S> A;
-    cpx<S> a0 = A::template fixdiv<5>(v[0]), a1 = A::template fixdiv<5>(v[VS]);
-    cpx<S> a2 = A::template fixdiv<5>(v[2 * VS]), a3 = A::template fixdiv<5>(v[3 * VS]);
-    cpx<S> a4 = A::template fixdiv<5>(v[4 * VS]);
-    cpx<S> t1 = A::cmul(a1, w[0]), t2 = A::cmul(a2, w[1]), t3 = A::cmul(a3, w[2]), t4 = A::cmul(a4, w[3]);
-    cpx<S> s14 = c_add(t1, t4), d14 = c_sub(t1, t4);
-    cpx<S> s23 = c_add(t2, t3), d23 = c_sub(t2, t3);
-    cpx<S> o0, b1, e1, b2, e2;
-    o0.r = A::st(A::add(a0.r, A::add(s14.r, s23.r)));
-    o0.i = A::st(A::add(a0.i, A::add(s14.i, s23.i)));
-    b1.r = A::st(A::add(A::add(a0.r, A::smul(s14.r, ya.r)), A::smul(s23.r, yb.r)));
-    b1.i = A::st(A::add(A::add(a0.i, A::smul(s14.i, ya.r)), A::smul(s23.i, yb.r)));
-    e1.r = A::st(A::add(A::smul(d14.i, ya.i), A::smul(d23.i, yb.i)));
-    e1.i = A::st(A::sub(A::neg(A::smul(d14.r, ya.i)), A::smul(d23.r, yb.i)));
-    b2.r = A::st(A::add(A::add(a0.r, A::smul(s14.r, yb.r)), A::smul(s23.r, ya.r)));
-    b2.i = A::st(A::add(A::add(a0.i, A::smul(s14.i, yb.r)), A::smul(s23.i, ya.r)));
-    e2.r = A::st(A::add(A::neg(A::smul(d14.i, yb.i)), A::smul(d23.i, ya.i)));
-    e2.i = A::st(A::sub(A::smul(d14.r, yb.i), A::smul(d23.r, ya.i)));
-    v[0] = o0;
-    v[VS] = c_sub(b1, e1);
-    v[4 * VS] = c_add(b1, e1);
-    v[2 * VS] = c_add(b2, e2);
-    v[3 * VS] = c_sub(b2, e2);
+    typedef typename A::CW CW;
+    typedef typename A::W W;
+    CW a0 = A::template fixdiv_w<5>(A::widen(v[0])), a1 = A::template fixdiv_w<5>(A::widen(v[VS]));
+    CW a2 = A::template fixdiv_w<5>(A::widen(v[2 * VS])), a3 = A::template fixdiv_w<5>(A::widen(v[3 * VS]));
+    CW a4 = A::template fixdiv_w<5>(A::widen(v[4 * VS]));
+    CW t1 = A::cmul_w(a1, w[0]), t2 = A::cmul_w(a2, w[1]), t3 = A::cmul_w(a3, w[2]), t4 = A::cmul_w(a4, w[3]);
+    CW s14 = w_add<S>(t1, t4), d14 = w_sub<S>(t1, t4);
+    CW s23 = w_add<S>(t2, t3), d23 = w_sub<S>(t2, t3);
+    const W s14r = A::tr(s14.r), s14i = A::tr(s14.i), s23r = A::tr(s23.r), s23i = A::tr(s23.i);
+    const W d14r = A::tr(d14.r), d14i = A::tr(d14.i), d23r = A::tr(d23.r), d23i = A::tr(d23.i);
+    CW o0, b1, e1, b2, e2;
+    o0.r = A::add(a0.r, A::add(s14r, s23r));
+    o0.i = A::add(a0.i, A::add(s14i, s23i));
+    b1.r = A::add(A::add(a0.r, A::smul_w(s14r, ya.r)), A::smul_w(s23r, yb.r));
+    b1.i = A::add(A::add(a0.i, A::smul_w(s14i, ya.r)), A::smul_w(s23i, yb.r));
+    e1.r = A::add(A::smul_w(d14i, ya.i), A::smul_w(d23i, yb.i));
+    e1.i = A::sub(A::neg(A::smul_w(d14r, ya.i)), A::smul_w(d23r, yb.i));
+    b2.r = A::add(A::add(a0.r, A::smul_w(s14r, yb.r)), A::smul_w(s23r, ya.r));
+    b2.i = A::add(A::add(a0.i, A::smul_w(s14i, yb.r)), A::smul_w(s23i, ya.r));
+    e2.r = A::add(A::neg(A::smul_w(d14i, yb.i)), A::smul_w(d23i, ya.i));
+    e2.i = A::sub(A::smul_w(d14r, yb.i), A::smul_w(d23r, ya.i));
+    v[0] = A::narrow(o0);
+    v[VS] = A::narrow(w_sub<S>(b1, e1));
+    v[4 * VS] = A::narrow(w_add<S>(b1, e1));
+    v[2 * VS] = A::narrow(w_add<S>(b2, e2));
+    v[3 * VS] = A::narrow(w_sub<S>(b2, e2));
 }
 
 template <typename S, int P, int VS>

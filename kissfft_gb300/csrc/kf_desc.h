@@ -33,6 +33,9 @@ enum { MODE_C2C = 0, MODE_R2C = 1, MODE_C2R = 2, MODE_FIR = 3 };
 enum { KIND_RT_GENERIC = 99 };
 // kernel families: the pass kinds a kernel is compiled for
 enum { FAM_POW2 = 0, FAM_SMOOTH = 1, FAM_GENERAL = 2 };
+// shared-tile index maps (all bijections inside blocks of 2^B elements):
+// three-level XOR fold, identity, one-level XOR
+enum { SWZ_FOLD = 0, SWZ_NONE = 1, SWZ_ONE = 2 };
 
 struct KStage {
     int p;       // radix
@@ -103,6 +106,7 @@ struct KArgs {
     const long long* out_off; // per-transform output base (elements)
     int tma;                  // 1: tiles are contiguous; stage the next tile by TMA bulk copy
     int stage_off;            // byte offset of the staging buffer in dynamic shared memory
+    int swz;                  // shared-tile layout: SWZ_FOLD, SWZ_NONE or SWZ_ONE (kf_engine.cuh swz)
     int* err;                 // device error word: bit 0 bad pass kind, bit 1 TMA wait timeout
 };
 

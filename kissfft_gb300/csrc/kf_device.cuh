@@ -94,7 +94,7 @@ struct DevExec {
 // through tiles blockIdx.x, blockIdx.x + gridDim.x, ... of J jobs each; the
 // tile lives in dynamic shared memory.  JF/CIF/COF > 0 fix the tile shape at
 // compile time (specialised kernels); 0 takes it from the arguments.
-template <typename S, int MODE, kmask_t KM, int JF = 0, int CIF = -1, int COF = -1>
+template <typename S, int MODE, kmask_t KM, int JF = 0, int CIF = -1, int COF = -1, int SWF = -1>
 __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, const KSub& s1) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
@@ -106,6 +106,7 @@ __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, cons
     const int co = COF >= 0 ? COF : a.col_out;
     Tile<S> t;
     tile_layout(a, s0.L, J, logJ, ci | co, t);
+    if (SWF >= 0) t.swzm = SWF;
     t.sm = (cpx<S>*)kf_dyn_smem;
     t.T = blockDim.x;
     t.inb = s_inb;
@@ -125,7 +126,7 @@ __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, cons
 // Tiles of contiguous input (a.tma): persistent CTAs, the next tile's input
 // is bulk-copied into a staging buffer while the current tile runs its
 // passes; the first pass reads the staged tile through shared memory.
-template <typename S, int MODE, kmask_t KM, int JF = 0>
+template <typename S, int MODE, kmask_t KM, int JF = 0, int SWF = -1>
 __device__ __forceinline__ void engine_body_tma(const KArgs& a, const KSub& s0) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
@@ -137,6 +138,7 @@ __device__ __forceinline__ void engine_body_tma(const KArgs& a, const KSub& s0) 
     cpx<S>* stage = (cpx<S>*)(kf_dyn_smem + a.stage_off);
     Tile<S> t;
     tile_layout(a, s0.L, J, logJ, 0, t);
+    if (SWF >= 0) t.swzm = SWF;
     t.sm = (cpx<S>*)kf_dyn_smem;
     t.T = blockDim.x;
     t.inb = s_inb;

@@ -31,7 +31,14 @@ struct alignas(16) uint4 {
 };
 #endif
 
+#ifndef KF_GEN_UNROLL
+#define KF_GEN_UNROLL 2
+#endif
+
 namespace kf {
+
+// unrolling of the output-leg loop of the fixed-point generic radix
+constexpr int kGenUnroll = KF_GEN_UNROLL;
 
 // Read-only (non-coherent cache) loads of tables: twiddles, reverse
 // tables.  The raw words go through aligned unions (no memcpy: NVRTC has no
@@ -120,10 +127,19 @@ struct SwzBits {
     static constexpr int v = sizeof(cpx<S>) == 4 ? 5 : (sizeof(cpx<S>) == 8 ? 4 : 3);
 };
 
-// XOR-fold swizzle inside aligned blocks of 2^B elements (a bijection).
+// Shared-tile index map inside aligned blocks of 2^B elements (a bijection):
+//   SWZ_FOLD  XOR of the three next digit groups into the low B bits --
+//             conflict-free sweeps for power-of-two strides;
+//   SWZ_ONE   XOR of the next digit group only (two instructions);
+//   SWZ_NONE  identity -- odd strides (generic radices) need no spreading,
+//             and integer-issue-bound fixed-point tiles gain more from the
+//             saved instructions than they lose to conflicts.
+// The launch picks the map (KArgs::swz; the autotuner times all three).
 template <typename S>
-KF_HD int swz(int I) {
+KF_HD int swz(int I, int mode) {
     constexpr int B = SwzBits<S>::v;
+    if (mode == SWZ_NONE) return I;
+    if (mode == SWZ_ONE) return I ^ ((I >> B) & ((1 << B) - 1));
     const int f = (I >> B) ^ (I >> (2 * B)) ^ (I >> (3 * B));
     return I ^ (f & ((1 << B) - 1));
 }
@@ -135,6 +151,7 @@ struct Tile {
     C* sm;
     int sA, sJ;  // shared index strides of the input-order index and of the job
     int J, logJ, col;
+    int swzm;    // index map (swz)
     int T;       // threads working on the tile
     int in_stride, out_stride;
     const long long* inb;
@@ -146,7 +163,7 @@ struct Tile {
     void* out;
     int* err;
 
-    KF_HD int sidx(int A, int job) const { return swz<S>(A * sA + job * sJ); }
+    KF_HD int sidx(int A, int job) const { return swz<S>(A * sA + job * sJ, swzm); }
     KF_HD C sld(int A, int job) const { return (KF_MEM_CHECK(sm + sidx(A, job), sizeof(C)), sm[sidx(A, job)]); }
     KF_HD void sst(int A, int job, C v) const { (KF_MEM_CHECK(sm + sidx(A, job), sizeof(C)), sm[sidx(A, job)] = v); }
     KF_HD bool valid(int job) const { return inb[job] >= 0; }
@@ -438,16 +455,17 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     typedef cpx<S> C;
     typedef Ar<S> Arr;
     constexpr bool kFixed = sizeof(typename Arr::W) == 4 && (S)0.5 == (S)0;
+    typedef typename Arr::CW CW;
     const KStage& sa = sb.st[ps.a];
     const C* tw = (const C*)tb.tw_full;
-    C x[P];
+    CW x[P];
     if (src_g) {
         const GIn<S, MODE> gi = gin<S, MODE>(t, g.job, g.A0);
 #pragma unroll
-        for (int q = 0; q < P; ++q) x[q] = Arr::template fixdiv<P>(gi.ld(q * sa.iloc));
+        for (int q = 0; q < P; ++q) x[q] = Arr::template fixdiv_w<P>(Arr::widen(gi.ld(q * sa.iloc)));
     } else {
 #pragma unroll
-        for (int q = 0; q < P; ++q) x[q] = Arr::template fixdiv<P>(t.sld(g.A0 + q * sa.iloc, g.job));
+        for (int q = 0; q < P; ++q) x[q] = Arr::template fixdiv_w<P>(Arr::widen(t.sld(g.A0 + q * sa.iloc, g.job)));
     }
     const int u = g.ul * sb.m_low + U;
     const int N = sb.N;
@@ -458,17 +476,37 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     if constexpr (kFixed) {
         typedef typename Arr::W W;
         constexpr int RP = gen_row(P);
-        const C* row = (const C*)tb.tw_stage + sa.tw_off + (long long)u * P * RP;
-#pragma unroll 1
-        for (int q1 = 0; q1 < P; ++q1) {
-            C w[RP];
-            ldro_vec<S, RP>(row + q1 * RP, w);
-            W ar = x[0].r, ai = x[0].i;
+        // twiddles as W pairs (Q15 rows are pre-widened, kf_shape.h gen_units)
+        const CW* row = (const CW*)((const C*)tb.tw_stage + sa.tw_off) + (long long)u * P * RP;
+#if defined(__CUDA_ARCH__)
+        // Q31: doubled legs for Ar::gen_out_q31
+        W x2r[P], x2i[P], x2n[P];
+        if constexpr (sizeof(S) == 4) {
 #pragma unroll
-            for (int q = 1; q < P; ++q) Arr::cmul_acc(ar, ai, x[q], w[q - 1]);
+            for (int q = 1; q < P; ++q) {
+                x2r[q] = (W)((unsigned)x[q].r << 1);
+                x2i[q] = (W)((unsigned)x[q].i << 1);
+                x2n[q] = (W)(0u - ((unsigned)x[q].i << 1));
+            }
+        }
+#endif
+#pragma unroll kGenUnroll
+        for (int q1 = 0; q1 < P; ++q1) {
+            CW w[RP];
+            ldro_vec<W, RP>(row + q1 * RP, w);
             C acc;
-            acc.r = Arr::st(ar);
-            acc.i = Arr::st(ai);
+#if defined(__CUDA_ARCH__)
+            if constexpr (sizeof(S) == 4) {
+                acc = Arr::template gen_out_q31<P>(x[0], x2r, x2i, x2n, w);
+            } else
+#endif
+            {
+                W ar = x[0].r, ai = x[0].i;
+#pragma unroll
+                for (int q = 1; q < P; ++q) Arr::cmul_acc_w(ar, ai, x[q], w[q - 1]);
+                acc.r = Arr::st(ar);
+                acc.i = Arr::st(ai);
+            }
             if (dst_g)
                 go.st(q1 * sa.mloc, acc);
             else
@@ -487,14 +525,14 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
             for (int q = 1; q < P; ++q) {
                 idx += step;
                 if (idx >= N) idx -= N;
-                x[q] = Arr::cmul(x[q], KF_LDG(tw + idx));
+                x[q] = Arr::cmul_w(x[q], KF_LDG(tw + idx));
             }
         }
-        C W[h + 1];
+        C Wr[h + 1];
 #pragma unroll
-        for (int r = 1; r <= h; ++r) W[r] = KF_LDG(tw + r * NP);
-        C a[h + 1], b[h + 1];
-        C y0 = x[0];
+        for (int r = 1; r <= h; ++r) Wr[r] = KF_LDG(tw + r * NP);
+        CW a[h + 1], b[h + 1];
+        CW y0 = x[0];
 #pragma unroll
         for (int q = 1; q <= h; ++q) {
             a[q].r = x[q].r + x[P - q].r;
@@ -507,14 +545,14 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
         y[0] = y0;
 #pragma unroll
         for (int q1 = 1; q1 <= h; ++q1) {
-            C A = x[0], B;
+            CW A = x[0], B;
             B.r = 0;
             B.i = 0;
 #pragma unroll
             for (int q = 1; q <= h; ++q) {
                 const int k = (q * q1) % P;
-                const S c = k <= h ? W[k].r : W[P - k].r;
-                const S sn = k <= h ? W[k].i : -W[P - k].i;
+                const S c = k <= h ? Wr[k].r : Wr[P - k].r;
+                const S sn = k <= h ? Wr[k].i : -Wr[P - k].i;
                 A.r += a[q].r * c;
                 A.i += a[q].i * c;
                 B.r += b[q].r * sn;

@@ -125,8 +125,16 @@ bool compile(const std::string& name, std::string& cubin, std::string& lowered, 
     }
     std::string expr = "&" + name;
     nvrtcAddNameExpression(prog, expr.c_str());
-    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true"};
-    nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
+    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true"};
+    // EXPERIMENT (to be removed): extra -D options for variant timing
+    std::vector<std::string> xdefs;
+    if (const char* e = getenv("KISSFFT_GB300_JIT_DEFS")) {
+        std::istringstream is(e);
+        std::string d;
+        while (is >> d) xdefs.push_back(d);
+    }
+    for (auto& d : xdefs) opts.push_back(d.c_str());
+    nvrtcResult r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     if (r != NVRTC_SUCCESS) {
         size_t n = 0;
         nvrtcGetProgramLogSize(prog, &n);
@@ -165,7 +173,7 @@ std::string spec_name(const Step& st) {
     std::ostringstream o;
     o << "kf::kf_spec_kernel<" << scalar_name(st.dtype) << "," << st.mode << "," << st.dtype << "," << st.shape_n
       << "," << st.shape_inv << ",0," << st.shape_sub << "," << st.args.J << "," << st.args.col_in << ","
-      << st.args.col_out << "," << st.cfg.T << "," << st.cfg.minb << ">";
+      << st.args.col_out << "," << st.cfg.T << "," << st.cfg.minb << "," << st.args.swz << ">";
     return o.str();
 }
 
@@ -195,7 +203,8 @@ const void* spec_kernel(const Step& st, std::string& err) {
     nvrtcVersion(&ver[0], &ver[1]);
     char key[64];
     snprintf(key, sizeof(key), "%016llx",
-             fnv1a(name + "|" + headers_digest() + "|sm_103a|" + std::to_string(ver[0] * 100 + ver[1])));
+             fnv1a(name + "|" + headers_digest() + "|sm_103a|" + std::to_string(ver[0] * 100 + ver[1]) + "|" +
+                   (getenv("KISSFFT_GB300_JIT_DEFS") ? getenv("KISSFFT_GB300_JIT_DEFS") : "")));
     const std::string dir = cache_dir();
     const std::string cpath = dir + "/" + key + ".cubin", npath = dir + "/" + key + ".name";
     std::string cubin, lowered;

@@ -232,7 +232,7 @@ struct kfg_plan {
     void* d_H = nullptr;
     // autotuned launch shapes per (batch, in_dist, out_dist): J, minb, tma per step
     std::mutex tune_mu;
-    std::map<std::string, std::vector<std::array<int, 5>>> tuned;
+    std::map<std::string, std::vector<std::array<int, 6>>> tuned;
     ~kfg_plan() {
         if (d_H) cudaFree(d_H);
     }
@@ -402,7 +402,7 @@ std::string tune_key(long long batch, long long in_dist, long long out_dist) {
     return o.str();
 }
 
-void apply_cfgs(Schedule& s, const std::vector<std::array<int, 5>>& v) {
+void apply_cfgs(Schedule& s, const std::vector<std::array<int, 6>>& v) {
     size_t k = 0;
     for (auto& st : s.steps) {
         if (st.kind != 0) continue;
@@ -414,6 +414,7 @@ void apply_cfgs(Schedule& s, const std::vector<std::array<int, 5>>& v) {
         // the tuning file is plain text on disk: take only budgets a launch can have
         if (c[1] >= 1 && c[1] <= 32) st.cfg.minb = c[1];
         st.tma_ok = c[2] != 0;
+        if (c[5] >= SWZ_FOLD && c[5] <= SWZ_ONE) st.args.swz = c[5];
     }
 }
 
@@ -435,7 +436,7 @@ std::string plan_sig(const kfg_plan* p) {
         snprintf(name, sizeof(name), "%s", prop.name);
     for (char* c = name; *c; ++c)
         if (*c == ' ') *c = '_';
-    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v4";
+    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v5";
     return o.str();
 }
 
@@ -451,7 +452,7 @@ std::string tune_file() {
     return d + "/tune.txt";
 }
 
-bool tune_load(const std::string& key, std::vector<std::array<int, 5>>& v) {
+bool tune_load(const std::string& key, std::vector<std::array<int, 6>>& v) {
     std::ifstream f(tune_file());
     std::string line;
     bool found = false;
@@ -459,16 +460,16 @@ bool tune_load(const std::string& key, std::vector<std::array<int, 5>>& v) {
         size_t sp = line.find(' ');
         if (sp == std::string::npos || line.compare(0, sp, key) != 0 || sp != key.size()) continue;
         std::istringstream is(line.substr(sp + 1));
-        std::vector<std::array<int, 5>> r;
-        std::array<int, 5> c;
-        while (is >> c[0] >> c[1] >> c[2] >> c[3] >> c[4]) r.push_back(c);
+        std::vector<std::array<int, 6>> r;
+        std::array<int, 6> c;
+        while (is >> c[0] >> c[1] >> c[2] >> c[3] >> c[4] >> c[5]) r.push_back(c);
         v = r;
         found = true;  // the last line for a key wins
     }
     return found;
 }
 
-void tune_store(const std::string& key, const std::vector<std::array<int, 5>>& v) {
+void tune_store(const std::string& key, const std::vector<std::array<int, 6>>& v) {
     std::string path = tune_file();
     std::string dir = path.substr(0, path.rfind('/'));
     std::string cmd;
@@ -476,7 +477,7 @@ void tune_store(const std::string& key, const std::vector<std::array<int, 5>>& v
         if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
     std::ofstream f(path, std::ios::app);
     f << key;
-    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2] << " " << c[3] << " " << c[4];
+    for (auto& c : v) f << " " << c[0] << " " << c[1] << " " << c[2] << " " << c[3] << " " << c[4] << " " << c[5];
     f << "\n";
 }
 
@@ -938,7 +939,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
     if (!p || batch < 1 || p->kind == K_FIR) return fail(KFG_EINVAL, "kfg_autotune: bad arguments");
     const std::string key = tune_key(batch, in_dist, out_dist);
     const std::string dkey = plan_sig(p) + ":" + key;
-    std::vector<std::array<int, 5>> best;
+    std::vector<std::array<int, 6>> best;
     if (tune_load(dkey, best)) {
         std::lock_guard<std::mutex> lk(p->tune_mu);
         p->tuned[key] = best;
@@ -1022,7 +1023,8 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
             for (auto& t : th) t.join();
         }
         float bt = -1.f;
-        std::array<int, 5> bc = {st0.cfg.J, st0.cfg.minb, 1, st0.args.col_in, st0.cfg.T};
+        std::array<int, 6> bc = {st0.cfg.J, st0.cfg.minb, 1, st0.args.col_in, st0.cfg.T, st0.args.swz};
+        Step bstep = st0;
         for (auto& c : cands) {
             for (int tma = 1; tma >= 0; --tma) {
                 Step x = c;
@@ -1030,15 +1032,42 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
                 float ms = time_step(x, roles, strm, e0, e1, 3);
                 if (ms > 0 && (bt < 0 || ms < bt)) {
                     bt = ms;
-                    bc = {c.cfg.J, c.cfg.minb, tma, c.args.col_in, c.cfg.T};
+                    bc = {c.cfg.J, c.cfg.minb, tma, c.args.col_in, c.cfg.T, c.args.swz};
+                    bstep = x;
                 }
                 if (!x.args.tma) break;  // staging not eligible: one timing is enough
+            }
+        }
+        // the winner's shape with the other shared-tile index maps
+        if (bt > 0) {
+            std::vector<Step> sw;
+            for (int m = SWZ_FOLD; m <= SWZ_ONE; ++m) {
+                if (m == bstep.args.swz) continue;
+                Step x = bstep;
+                x.args.swz = m;
+                sw.push_back(x);
+            }
+            if (specialize_enabled()) {
+                std::vector<std::thread> th;
+                for (auto& c : sw)
+                    th.emplace_back([&c]() {
+                        std::string err;
+                        spec_kernel(c, err);
+                    });
+                for (auto& t : th) t.join();
+            }
+            for (auto& x : sw) {
+                float ms = time_step(x, roles, strm, e0, e1, 3);
+                if (ms > 0 && ms < bt) {
+                    bt = ms;
+                    bc[5] = x.args.swz;
+                }
             }
         }
         best.push_back(bc);
         // later steps read what this one wrote: run it once with the winner
         Step w = st0;
-        std::vector<std::array<int, 5>> one = {bc};
+        std::vector<std::array<int, 6>> one = {bc};
         Schedule tmp;
         tmp.steps.push_back(w);
         apply_cfgs(tmp, one);

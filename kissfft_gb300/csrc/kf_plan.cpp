@@ -136,7 +136,15 @@ bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
                     long long idx = 0;
                     for (int q = 1; q < p; ++q) {
                         idx = (idx + step) % n;
-                        memcpy(base + (size_t)((u * p + q1) * RP + (q - 1)) * esz, twf.data() + (size_t)idx * esz, esz);
+                        const size_t slot = (size_t)((u * p + q1) * RP + (q - 1));
+                        if (dtype == KF_Q15) {
+                            // sign-extended int32 pair (kf_shape.h gen_units)
+                            const int16_t* w = (const int16_t*)(twf.data() + (size_t)idx * esz);
+                            const int32_t pair[2] = {w[0], w[1]};
+                            memcpy(base + slot * 8, pair, 8);
+                        } else {
+                            memcpy(base + slot * esz, twf.data() + (size_t)idx * esz, esz);
+                        }
                     }
                 }
             continue;
@@ -353,7 +361,18 @@ bool reshape_step(Step& st, int J) {
     return true;
 }
 
+// Default shared-tile index map of a launch (kf_engine.cuh swz): the
+// XOR fold for IEEE tiles whose strides are even; none for odd-length
+// (generic-radix) tiles and for fixed point, whose integer-issue-bound
+// passes gain more from the saved instructions than they lose to bank
+// conflicts (measured over the 480/1000/3003/65536 workload).
+int default_swz(int dtype, int L) {
+    if (dtype == KF_Q15 || dtype == KF_Q31) return SWZ_NONE;
+    return (L & 1) ? SWZ_NONE : SWZ_FOLD;
+}
+
 static void finish(Step& st, const LaunchCfg& c) {
+    st.args.swz = default_swz(st.dtype, st.args.sub[0].L);
     st.fam = sub_family(st.args.sub[0]);
     if (st.args.nsub > 1) st.fam = std::max(st.fam, sub_family(st.args.sub[1]));
     st.cfg = c;

@@ -70,6 +70,8 @@ struct Plan {
 LaunchCfg default_cfg(const KSub& sb, int dtype, int mode, long long G, int col_in, int col_out, int want_threads = 256);
 int cfg_smem_bytes(const KSub& sb, int dtype, int J);
 int cfg_min_threads(const KSub& sb, int mode, int J);
+// Default shared-tile index map (SWZ_*) of a launch over tiles of length L.
+int default_swz(int dtype, int L);
 // Smallest kernel family whose compiled pass kinds cover a sub-plan.
 int sub_family(const KSub& sb);
 

@@ -76,6 +76,7 @@ KF_HD void tile_layout(const KArgs& a, int L, int J, int logJ, int col, Tile<S>&
     }
     t.in = a.in;
     t.out = a.out;
+    t.swzm = a.swz;
     t.in_stride = (int)a.in_stride;
     t.out_stride = (int)a.out_stride;
     t.err = a.err;

@@ -47,8 +47,12 @@ KF_CX bool small_prime(int p) {
 // Fixed-point generic-radix stages (p = 7..31) read their twiddles from
 // rows: for every u < m and output leg q1 < p, gen_row(p) consecutive
 // entries tw[(q*fstride*(u + q1*m)) mod N] for q = 1..p-1 (then padding) --
-// the exact sequence kf_bfly_generic walks (kiss_fft.c:218-226).
+// the exact sequence kf_bfly_generic walks (kiss_fft.c:218-226).  Q15 rows
+// hold each twiddle as a pair of int32 (the 16-bit values sign-extended, so
+// the multiplies take them as they are): gen_units(dtype) table entries
+// per twiddle.
 KF_CX int gen_row(int p) { return (p - 1 + 3) & ~3; }
+KF_CX int gen_units(int dtype) { return dtype == KF_Q15 ? 2 : 1; }
 
 // magic multiplier M with n / d == (n * M) >> 40 for n * d < 2^40
 KF_CX unsigned long long div_magic(int d) {
@@ -191,7 +195,7 @@ KF_CX ShapeInfo make_shape(int dtype, int n, int inverse, int lmax, int real_nff
         } else if ((dtype == KF_Q15 || dtype == KF_Q31) && small_prime(f[j])) {
             cnt = (cnt + 3) & ~3LL;
             si.twoff[j] = (int)cnt;
-            cnt += (long long)gen_row(f[j]) * f[j] * si.m[j];
+            cnt += (long long)gen_row(f[j]) * f[j] * si.m[j] * gen_units(dtype);
         } else {
             si.twoff[j] = -1;
         }

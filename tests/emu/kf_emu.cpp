@@ -59,7 +59,7 @@ struct EmuOwn {
 
 using namespace kf;
 
-static int g_force_J = 0, g_force_T = 0, g_force_col = 0;
+static int g_force_J = 0, g_force_T = 0, g_force_col = 0, g_force_swz = -1;
 
 template <typename S, int MODE, kmask_t KM>
 struct CpuExec {
@@ -168,6 +168,7 @@ static int run_schedule(Schedule& s, const void* in, void* out, const void* firH
             st.cfg.T = std::max(st.cfg.T, cfg_min_threads(st.args.sub[0], st.mode, g_force_J));
         }
         if (g_force_T && st.kind == 0) st.cfg.T = std::max(g_force_T, cfg_min_threads(st.args.sub[0], st.mode, st.cfg.J));
+        if (g_force_swz >= 0 && st.kind == 0) st.args.swz = g_force_swz;
         if (g_force_col && st.kind == 0 && st.mode != MODE_FIR) {
             st.cfg.col_in = st.cfg.col_out = 1;
             st.args.col_in = st.args.col_out = 1;
@@ -212,6 +213,9 @@ void emu_force(int J, int T) {
 
 // column-layout tiles (jobs fastest) for every engine step
 void emu_force_col(int col) { g_force_col = col; }
+
+// shared-tile index map (SWZ_*) of every engine step; -1: the schedule's own
+void emu_force_swz(int mode) { g_force_swz = mode; }
 
 int emu_c2c(int dtype, int n, int inverse, int lmax, const void* in, void* out, long long batch, long long in_dist,
             long long in_stride, long long out_dist) {

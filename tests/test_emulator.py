@@ -166,6 +166,35 @@ def test_forced_tile_shapes(emu):
             emu.emu_force(0, 0)
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
+def test_shared_index_maps(emu, dtype, mode):
+    """Every shared-tile index map (XOR fold, identity, one-level XOR) on row
+    and column tiles, real transforms included, gives the oracle's bits."""
+    emu.emu_force_swz(mode)
+    try:
+        for col in (0, 1):
+            emu.emu_force_col(col)
+            for n in (30, 480, 1000, 3003, 1024, 65536):
+                x = inputs.cpx((6, n), dtype, n + mode)
+                y = np.zeros_like(x)
+                assert emu.emu_c2c(DT[dtype], n, 0, 0, p(x), p(y), L(6), L(n), L(1), L(n)) == 0
+                check(y, lambda: kfo.fft(x, 0, dtype), x, dtype, n, 0)
+            for nfft in (480, 4096, 6006):
+                t = inputs.real((3, nfft), dtype, nfft)
+                f = kfo.empty_cpx((3, nfft // 2 + 1), dtype)
+                assert emu.emu_r2c(DT[dtype], nfft, 0, p(t), p(f), L(3)) == 0
+                if fixed(dtype):
+                    assert np.array_equal(f, kfo.fftr(t, dtype)), (mode, col, nfft)
+                else:
+                    ex = np.fft.rfft(t.astype(np.float64), axis=-1)
+                    e = np.max(np.linalg.norm(f - ex, axis=-1) / np.linalg.norm(ex, axis=-1))
+                    assert e <= 2e-7 * np.log2(nfft), (mode, col, nfft, e)
+    finally:
+        emu.emu_force_col(0)
+        emu.emu_force_swz(-1)
+
+
 @pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
 def test_column_tiles_on_row_batches(emu, dtype):
     """Column-layout tiles (jobs fastest in shared memory) on row-major
