@@ -333,9 +333,12 @@ def run_gpu(args):
         from oracle import kfo
         nth = kfo.max_threads()
         g, secs, passes = run_cpu(host_in, nth, args.cpu_seconds)
+        gp, secs_p, passes_p = run_cpu(host_in, nth, min(5.0, args.cpu_seconds), release=False)
         cpu = {"value": round(g, 3), "unit": "GB/s", "cores": nth, "kind": "port",
                "sample": "the whole workload (all 12 batches) %d time(s), %.1f s of CPU work" % (passes, secs),
-               "form": "OpenMP over the transforms of each batch (one plan per thread)"}
+               "form": "OpenMP over the transforms of each batch (one plan per thread)", "build": REL_BUILD,
+               "parity_build": {"value": round(gp, 3), "build": PARITY_BUILD,
+                                "sample": "the whole workload %d time(s), %.1f s" % (passes_p, secs_p)}}
         cpu["openmp_build"] = legs_entry(host_in, nth, min(3.0, args.cpu_seconds), 1.0 / 64)
     gflops = sum(c2c_flops(n, b) for dt, n, b in us) / (ms * 1e-3) / 1e9
     return {"value": value, "gflops": gflops, "ms": ms, "units": unit_rows, "roofline": roof, "e2e": e2e,
@@ -647,18 +650,23 @@ def run_serving(args):
 
 
 # ------------------------------------------------------------------ CPU arm
-def run_cpu(host_in, nthreads, min_seconds):
+REL_BUILD = "-O3 -ffast-math -fomit-frame-pointer (the reference's CMake release flags, CMakeLists.txt:98-102)"
+PARITY_BUILD = "-O2 -ffp-contract=off (the parity build the tests check against)"
+
+
+def run_cpu(host_in, nthreads, min_seconds, release=True):
     """The oracle (CPU restatement of the reference path, OpenMP over the
     transforms of a batch) on the bench's own input batches, whole passes
     repeated until at least min_seconds of wall time; returns GB/s of
-    compulsory bytes, the seconds and the passes."""
+    compulsory bytes, the seconds and the passes.  release: the build at the
+    reference's release flags (else the -O2 parity build)."""
     from oracle import kfo
     us = units()
     tot_bytes, tot_s, passes = 0, 0.0, 0
     while tot_s < min_seconds or passes == 0:
         for x, (dt, n, b) in zip(host_in, us):
             ts = time.perf_counter()
-            kfo.fft(x, 0, dt, nthreads=nthreads)
+            kfo.fft(x, 0, dt, nthreads=nthreads, release=release)
             tot_s += time.perf_counter() - ts
             tot_bytes += 2 * n * ESZ[dt] * b
         passes += 1
@@ -678,7 +686,7 @@ def run_cpu_legs(host_in, nthreads, min_seconds, frac=1.0 / 64):
     while tot_s < min_seconds or passes == 0:
         for x, dt, n, k in parts:
             ts = time.perf_counter()
-            kfo.fft_legs(x, 0, dt, nthreads=nthreads)
+            kfo.fft_legs(x, 0, dt, nthreads=nthreads, release=True)
             tot_s += time.perf_counter() - ts
             tot_bytes += 2 * n * ESZ[dt] * k
         passes += 1
@@ -747,6 +755,7 @@ def main():
             g, s, _p = run_cpu(host_in, nth, 0)
             per.append(g)
         v = statistics.median(per)
+        gp, _s, _p = run_cpu(host_in, nth, 0, release=False)
         sample = "each step: one pass over %s of every batch (%d transforms)" % (
             "all" if args.cpu_frac >= 1 else "1/%d" % round(1 / args.cpu_frac), sum(b for _, _, b in _CASES))
         line = {"impl": "reference", "metric": "HBM GB/s (compulsory bytes), batched FFT", "value": round(v, 3),
@@ -756,6 +765,9 @@ def main():
                 "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": nth, "kind": "port",
                                  "sample": sample,
                                  "form": "OpenMP over the transforms of each batch (one plan per thread)",
+                                 "build": REL_BUILD,
+                                 "parity_build": {"value": round(gp, 3), "build": PARITY_BUILD,
+                                                  "sample": "one pass of the same sample"},
                                  "openmp_build": legs_entry(host_in, nth, 3.0, 1.0 / 8, args.cpu_frac)},
                 "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))

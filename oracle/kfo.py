@@ -23,8 +23,14 @@ CPLX = {"float": np.complex64, "double": np.complex128}
 # counts the fixed-point overflows the reference's CHECK_OVERFLOW warns about
 LIB_OVF_PATH = os.path.join(HERE, "_build", "libkfo_ovf.so")
 
+# the same restatement compiled at the reference's release flags
+# (-O3 -ffast-math -fomit-frame-pointer, CMakeLists.txt:98-102): used only to
+# time the CPU baseline, never as the checker
+LIB_REL_PATH = os.path.join(HERE, "_build", "libkfo_rel.so")
+
 _lib = None
 _lib_ovf = None
+_lib_rel = None
 _override = None  # set by overflows() while it runs
 
 
@@ -60,6 +66,13 @@ def lib_ovf():
     if _lib_ovf is None:
         _lib_ovf = _load(LIB_OVF_PATH)
     return _lib_ovf
+
+
+def lib_rel():
+    global _lib_rel
+    if _lib_rel is None:
+        _lib_rel = _load(LIB_REL_PATH)
+    return _lib_rel
 
 
 def overflows(fn, *args, **kwargs):
@@ -134,18 +147,19 @@ def super_twiddles(nfft, inverse, dtype):
     return out
 
 
-def fft(x, inverse=False, dtype="float", nthreads=1):
-    """Batched complex transform along the last (complex) axis."""
+def fft(x, inverse=False, dtype="float", nthreads=1, release=False):
+    """Batched complex transform along the last (complex) axis.  release=True
+    runs the release-flags build (timing only)."""
     x = as_cpx(x, dtype)
     n = x.shape[-2] if is_fixed(dtype) else x.shape[-1]
     batch = x.size // (2 * n if is_fixed(dtype) else n)
     out = np.empty_like(x)
-    getattr(lib(), "kfo_fft_batch_" + SFX[dtype])(int(n), int(bool(inverse)), _p(x), _p(out),
+    getattr(lib_rel() if release else lib(), "kfo_fft_batch_" + SFX[dtype])(int(n), int(bool(inverse)), _p(x), _p(out),
                                                    ctypes.c_long(batch), int(nthreads))
     return out
 
 
-def fft_legs(x, inverse=False, dtype="float", nthreads=1):
+def fft_legs(x, inverse=False, dtype="float", nthreads=1, release=False):
     """Batched complex transform with the reference's KISSFFT_OPENMP split:
     transforms one after the other, the top-level legs of each in parallel
     (kiss_fft.c:250-272).  Same results as fft()."""
@@ -153,7 +167,7 @@ def fft_legs(x, inverse=False, dtype="float", nthreads=1):
     n = x.shape[-2] if is_fixed(dtype) else x.shape[-1]
     batch = x.size // (2 * n if is_fixed(dtype) else n)
     out = np.empty_like(x)
-    rc = getattr(lib(), "kfo_fft_batch_legs_" + SFX[dtype])(int(n), int(bool(inverse)), _p(x), _p(out),
+    rc = getattr(lib_rel() if release else lib(), "kfo_fft_batch_legs_" + SFX[dtype])(int(n), int(bool(inverse)), _p(x), _p(out),
                                                              ctypes.c_long(batch), int(nthreads))
     if rc != 0:
         raise MemoryError("kfo_fft_batch_legs: scratch allocation failed")
