@@ -456,13 +456,16 @@ def run_mix(args, count=MIX_COUNT):
             av, bv = a.view(torch.float32).double(), b.view(torch.float32).double()
             worst = max(worst, float((av - bv).norm() / bv.norm().clamp_min(1e-30)))
     L.kfg_batch_free(B)
+    single = percall_single(L, st)
     distinct = len(set((r[0], r[1], r[2]) for r in reqs))
     return {"workload": "uneven mix: %d requests, nfft log-uniform [16, 131072], 80%% 2^a3^b5^c / 20%% with a "
                         "prime 7..31; 60%% c2c f32, 30%% r2c f32, 10%% c2c Q15; seed 3" % count,
             "requests": count, "distinct_plans": distinct, "compulsory_bytes": alg,
             "graph": {"ms": round(graph_ms, 3), "gbs": round(alg / graph_ms / 1e6, 1)},
             "direct": {"ms": round(direct_ms, 3), "gbs": round(alg / direct_ms / 1e6, 1)},
-            "percall": {"ms": round(percall_ms, 3), "gbs": round(alg / percall_ms / 1e6, 1)},
+            "percall": {"ms": round(percall_ms, 3), "gbs": round(alg / percall_ms / 1e6, 1),
+                        "us_per_request": round(percall_ms * 1e3 / count, 2)},
+            "percall_us": single,
             "speedup_vs_percall": round(percall_ms / graph_ms, 2),
             "autotuned_target_threads": target, "launches": int(info[2]), "tiles": int(info[3]),
             "max_rel_diff_vs_percall": worst, "commit_and_tune_s": round(t_commit, 2)}
@@ -647,6 +650,34 @@ def run_serving(args):
                         "gbs": round(poisson["percall_gbs"], 2), "p50_ms": round(poisson["percall_p50_s"] * 1e3, 3),
                         "p99_ms": round(poisson["percall_p99_s"] * 1e3, 3)},
             "saturated_vs_percall": round(ss["req_per_s"] / max(poisson["percall_req_per_s"], 1e-9), 2)}
+
+
+def percall_single(L, st, n=1024, calls=5000):
+    """Host cost of one plain drop-in call: a 1024-point float forward
+    transform on device buffers (kfg_exec, enqueued on the stream), timed
+    over `calls` back-to-back calls from Python (ctypes), with the cost of a
+    ctypes call that does nothing beside it."""
+    import ctypes
+    import torch
+    vp = ctypes.c_void_p
+    p = L.kfg_plan_c2c(0, n, 0)
+    x = torch.randn(2 * n, device="cuda")
+    y = torch.empty_like(x)
+    xa, ya = vp(x.data_ptr()), vp(y.data_ptr())
+    for _ in range(50):
+        L.kfg_exec(p, xa, ya, st)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        L.kfg_exec(p, xa, ya, st)
+    t1 = time.perf_counter()
+    torch.cuda.synchronize()
+    for _ in range(calls):
+        L.kfg_get_stream()
+    t2 = time.perf_counter()
+    L.kfg_plan_free(p)
+    return {"nfft": n, "us": round((t1 - t0) / calls * 1e6, 2), "python_ctypes_us": round((t2 - t1) / calls * 1e6, 2),
+            "calls": calls, "what": "kfg_exec on device buffers, host time per call including the Python call"}
 
 
 # ------------------------------------------------------------------ CPU arm

@@ -145,6 +145,7 @@ inline cudaError_t launch_spec(const void* k, const Step& st, cudaStream_t s) {
 
 inline cudaError_t launch_step(const Step& st, cudaStream_t s) {
     if (st.kind == 0 && specialize_enabled()) {
+        if (st.kfn) return launch_spec(st.kfn, st, s);
         std::string err;
         const void* k = spec_kernel(st, err);
         if (k) return launch_spec(k, st, s);

@@ -222,6 +222,15 @@ __global__ void kf_scale_kernel(float* H, long long n, float s) {
 
 }  // namespace
 
+// A call's launch schedule, tuned and with its specialised kernels resolved,
+// kept per plan for the next call of the same shape.
+struct CachedSched {
+    long long batch, in_dist, in_stride, out_dist;
+    Schedule s;
+    size_t ib = 0, ob = 0;
+    bool multi = false;  // several steps or column tiles (the pinned-host copy pipeline qualifies)
+};
+
 struct kfg_plan {
     int kind = 0, dtype = 0, inverse = 0;
     long long n = 0;  // c2c: nfft; real: nfft; nd/ndr: product of dims; fir: nfft
@@ -230,6 +239,9 @@ struct kfg_plan {
     std::vector<std::unique_ptr<DevPlan>> axes;  // one per axis (nd), or per leading axis (ndr)
     long long ntaps = 0;
     void* d_H = nullptr;
+    // ready launch schedules of recent calls (most recent first)
+    std::mutex sched_mu;
+    std::vector<std::shared_ptr<const struct CachedSched>> scheds;
     // autotuned launch shapes per (batch, in_dist, out_dist): J, minb, tma per step
     std::mutex tune_mu;
     std::map<std::string, std::vector<std::array<int, 6>>> tuned;
@@ -396,6 +408,55 @@ int exec_staged(Schedule& s, const void* in, void* out, size_t in_bytes, size_t 
 
 bool valid_dtype(int d) { return d >= KFG_FLOAT && d <= KFG_INT32; }
 
+constexpr size_t kSchedCache = 8;
+
+void apply_tuned(kfg_plan* p, const std::string& key, Schedule& s);
+std::string tune_key(long long batch, long long in_dist, long long out_dist);
+
+// The schedule of a call of this shape: from the plan's cache, or built,
+// tuned (for unit stride), its specialised kernels resolved, and cached.  A
+// plain device-pointer call then costs little more than its launches.
+int get_schedule(kfg_plan* p, long long batch, long long in_dist, long long in_stride, long long out_dist,
+                 std::shared_ptr<const CachedSched>& out) {
+    {
+        std::lock_guard<std::mutex> lk(p->sched_mu);
+        for (size_t i = 0; i < p->scheds.size(); ++i) {
+            const auto& c = p->scheds[i];
+            if (c->batch == batch && c->in_dist == in_dist && c->in_stride == in_stride && c->out_dist == out_dist) {
+                out = c;
+                if (i) std::rotate(p->scheds.begin(), p->scheds.begin() + i, p->scheds.begin() + i + 1);
+                return KFG_OK;
+            }
+        }
+    }
+    auto c = std::make_shared<CachedSched>();
+    c->batch = batch;
+    c->in_dist = in_dist;
+    c->in_stride = in_stride;
+    c->out_dist = out_dist;
+    int rc = build_schedule(p, batch, in_dist, in_stride, out_dist, c->s, c->ib, c->ob);
+    if (rc) return rc;
+    if (in_stride == 1) apply_tuned(p, tune_key(batch, in_dist, out_dist), c->s);
+    c->multi = c->s.steps.size() > 1;
+    for (auto& st : c->s.steps) {
+        c->multi |= st.args.col_in || st.args.col_out;
+        if (st.kind == 0 && specialize_enabled()) {
+            std::string err;
+            st.kfn = spec_kernel(st, err);  // null: the precompiled kernels run
+        }
+    }
+    out = c;
+    std::lock_guard<std::mutex> lk(p->sched_mu);
+    p->scheds.insert(p->scheds.begin(), c);
+    if (p->scheds.size() > kSchedCache) p->scheds.resize(kSchedCache);
+    return KFG_OK;
+}
+
+void drop_schedules(kfg_plan* p) {
+    std::lock_guard<std::mutex> lk(p->sched_mu);
+    p->scheds.clear();
+}
+
 std::string tune_key(long long batch, long long in_dist, long long out_dist) {
     std::ostringstream o;
     o << batch << "/" << in_dist << "/" << out_dist;
@@ -415,6 +476,7 @@ void apply_cfgs(Schedule& s, const std::vector<std::array<int, 6>>& v) {
         if (c[1] >= 1 && c[1] <= 32) st.cfg.minb = c[1];
         st.tma_ok = c[2] != 0;
         if (c[5] >= SWZ_FOLD && c[5] <= SWZ_ONE) st.args.swz = c[5];
+        st.kfn = nullptr;
     }
 }
 
@@ -777,21 +839,19 @@ int kfg_exec_batch(kfg_plan* p, const void* in, void* out, long long batch, long
     if (!p || !in || !out || batch < 0) return fail(KFG_EINVAL, "kfg_exec_batch: bad arguments");
     if (batch == 0) return KFG_OK;
     if (p->kind == K_FIR) return fail(KFG_EINVAL, "use kfg_fir_filter for a fast FIR plan");
-    Schedule s;
-    size_t ib = 0, ob = 0;
-    int rc = build_schedule(p, batch, in_dist, 1, out_dist, s, ib, ob);
+    std::shared_ptr<const CachedSched> c;
+    int rc = get_schedule(p, batch, in_dist, 1, out_dist, c);
     if (rc) return rc;
-    apply_tuned(p, tune_key(batch, in_dist, out_dist), s);
     // pinned host buffers: kernels that read whole rows in one pass use
     // them in place (zero-copy); schedules of several steps or column tiles
     // (short runs per row over the host link) take the copy pipeline
-    bool multi = s.steps.size() > 1;
-    for (auto& st : s.steps) multi |= st.args.col_in || st.args.col_out;
-    if (multi && pipeline_enabled() && is_pinned_host_ptr(in) && is_pinned_host_ptr(out) && (const void*)out != in) {
+    if (c->multi && pipeline_enabled() && is_pinned_host_ptr(in) && is_pinned_host_ptr(out) &&
+        (const void*)out != in) {
         rc = exec_pipelined(p, in, out, batch, in_dist, out_dist, pick(stream));
         if (rc != 1) return rc;
     }
-    return exec_staged(s, in, out, ib, ob, pick(stream));
+    Schedule s = c->s;  // the executor writes buffer pointers into its copy
+    return exec_staged(s, in, out, c->ib, c->ob, pick(stream));
 }
 
 int kfg_exec(kfg_plan* p, const void* in, void* out, void* stream) { return kfg_exec_batch(p, in, out, 1, 0, 0, stream); }
@@ -799,11 +859,11 @@ int kfg_exec(kfg_plan* p, const void* in, void* out, void* stream) { return kfg_
 int kfg_exec_stride(kfg_plan* p, const void* in, void* out, int in_stride, void* stream) {
     if (!p || !in || !out || in_stride < 1) return fail(KFG_EINVAL, "kfg_exec_stride: bad arguments");
     if (p->kind != K_C2C) return fail(KFG_EINVAL, "kfg_exec_stride needs a complex 1-D plan");
-    Schedule s;
-    size_t ib = 0, ob = 0;
-    int rc = build_schedule(p, 1, 0, in_stride, 0, s, ib, ob);
+    std::shared_ptr<const CachedSched> c;
+    int rc = get_schedule(p, 1, 0, in_stride, 0, c);
     if (rc) return rc;
-    return exec_staged(s, in, out, ib, ob, pick(stream));
+    Schedule s = c->s;
+    return exec_staged(s, in, out, c->ib, c->ob, pick(stream));
 }
 
 int kfg_fir_filter(kfg_plan* p, const float* x, size_t nx, float* y, size_t* ny_out, void* stream) {
@@ -941,8 +1001,11 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
     const std::string dkey = plan_sig(p) + ":" + key;
     std::vector<std::array<int, 6>> best;
     if (tune_load(dkey, best)) {
-        std::lock_guard<std::mutex> lk(p->tune_mu);
-        p->tuned[key] = best;
+        {
+            std::lock_guard<std::mutex> lk(p->tune_mu);
+            p->tuned[key] = best;
+        }
+        drop_schedules(p);
         return KFG_OK;
     }
     Schedule s;
@@ -1084,6 +1147,7 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
         std::lock_guard<std::mutex> lk(p->tune_mu);
         p->tuned[key] = best;
     }
+    drop_schedules(p);
     tune_store(dkey, best);
     return KFG_OK;
 }

@@ -319,6 +319,7 @@ bool recolumn_step(Step& st) {
     st.cfg.col_in = st.cfg.col_out = 1;
     st.args.col_in = st.args.col_out = 1;
     st.args.tma = 0;
+    st.kfn = nullptr;
     return true;
 }
 
@@ -338,6 +339,7 @@ bool retarget_threads(Step& st, int T) {
     if (T < cfg_min_threads(st.args.sub[0], st.mode, st.cfg.J)) return false;
     st.cfg.T = T;
     st.cfg.minb = default_minb(T, st.cfg.smem);
+    st.kfn = nullptr;
     return true;
 }
 
@@ -372,6 +374,7 @@ int default_swz(int dtype, int L) {
 }
 
 static void finish(Step& st, const LaunchCfg& c) {
+    st.kfn = nullptr;
     st.args.swz = default_swz(st.dtype, st.args.sub[0].L);
     st.fam = sub_family(st.args.sub[0]);
     if (st.args.nsub > 1) st.fam = std::max(st.fam, sub_family(st.args.sub[1]));

@@ -102,6 +102,9 @@ struct Step {
     LaunchCfg cfg;
     // buffer roles resolved by the executor: 0 user in, 1 user out, 2 tmp
     int in_role = 0, out_role = 1;
+    // run-time specialised kernel resolved for exactly this launch shape
+    // (set by the executor's schedule cache; any change of the shape clears it)
+    const void* kfn = nullptr;
 };
 
 // Buffer roles of a schedule: 0 the caller's input, 1 the caller's output,

@@ -85,7 +85,8 @@ def test_gpu_arm_runs_through_on_cpu_stand_ins():
     run, line = res["run"], res["line"]
     assert len(run["units"]) == 4
     for u in run["units"]:
-        assert u["gbs"] > 0 and u["gflops_5nlog2n"] > 0
+        # stand-in timings of a busy host can round the rates to 0.0
+        assert u["ms"] > 0 and u["gbs"] >= 0 and u["gflops_5nlog2n"] >= 0
         a = u["accuracy"]
         if u["dtype"] == "float":
             # the stand-in is the oracle itself: its error is the reference float build's
