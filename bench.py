@@ -19,7 +19,9 @@ Printed JSON line (one, on rank 0):
           reference float build's own error on the same rows; Q15/Q31
           bit-exactness against the reference's fixed-point arithmetic
   e2e     the same through the drop-in C ABI with host (pinned) buffers,
-          host<->device copies inside the timed region
+          host<->device copies inside the timed region; its "link" entry is
+          the measured copy-engine peak of the host link and the step's
+          fraction of it
   roofline  the dominant kernel's achieved GB/s (its compulsory bytes per
           launch / its CUDA-event launch time) against the measured HBM peak
   cpu_baseline  the CPU restatement of the reference path (oracle/, OpenMP
@@ -29,8 +31,9 @@ Printed JSON line (one, on rank 0):
           parallel) on a 1/64 sample
   batched_mix  the uneven-size mix (20,000 requests) as one batch replayed
           from a CUDA graph against the plain per-call form
-  serving  the serving loop under Poisson arrivals: p50/p99 latency and
-          throughput, saturated throughput, and the per-call form
+  serving  the serving loop under Poisson arrivals offered at 50k..500k
+          requests/s and held at 50k for 60 s: p50/p99 latency, throughput,
+          host-link GB/s, saturated throughput, and the per-call form
   other_configs  the 1024-point round trip, real 4096 x 65536 forward and
           inverse, 2-D 2048^2 and real 3-D 128^3, each timed alone
 
@@ -315,6 +318,10 @@ def run_gpu(args):
                        "host link; two-pass and column-tile schedules run a chunked copy-in / kernels / copy-out "
                        "pipeline on three streams",
                "units": e_units}
+        link = link_peak()
+        moved = (h2d + h2d) / (e_ms * 1e-3) / 1e9  # host-link bytes of a step, both directions
+        e2e["link"] = dict(link, step_link_gbs=round(moved, 1),
+                           frac=round(moved / link["bidir_gbs"], 3) if link["bidir_gbs"] > 0 else None)
         # the e2e output must equal the device-resident output
         for i in range(len(us)):
             if not torch.equal(hout[i], ys[i].cpu()):
@@ -616,13 +623,16 @@ def run_configs(args):
 
 # ------------------------------------------------------------------ serving loop
 def run_serving(args):
-    """Serving loop (kfg_server, 40 GB HBM budget): Poisson arrivals at
-    50,000 requests/s for 5 s of a mix of c2c (N log-uniform 64..65536),
-    r2c, 2-D (256..1024 per side) and fast-FIR (255..4095 taps, 2^16..2^22
-    samples) requests in equal shares (seed 4), inputs and outputs in pinned
-    host memory; then the same mix submitted all at once (the loop's
-    saturated throughput); then the first 2,000 requests through the plain
-    per-call form.  Latency is submit to completion, p50/p99."""
+    """Serving loop (kfg_server, 40 GB HBM budget) on a mix of c2c (N
+    log-uniform 64..65536), r2c, 2-D (256..1024 per side) and fast-FIR
+    (255..4095 taps, 2^16..2^22 samples) requests in equal shares (seed 4),
+    inputs and outputs in pinned host memory: Poisson arrivals offered at
+    50k, 100k, 200k and 500k requests/s (each for at most 3 s and 150,000
+    requests), then held at 50,000 requests/s for --serve-hold seconds
+    (default 60); then the same mix submitted all at once (the loop's
+    saturated throughput); then the first 2,000 requests of the held run
+    through the plain per-call form.  Latency is submit to completion,
+    p50/p99; link_gbs counts the requests' bytes over the host link."""
     import kissfft_gb300 as kf
 
     kf.set_specialize(False)
@@ -630,19 +640,23 @@ def run_serving(args):
     try:
         # warm the device plan cache with the mix's sizes (a burst of the same seed)
         srv.loadtest(rate=0.0, count=5000, seed=4, percall_max=0)
-        poisson = srv.loadtest(rate=50000.0, seconds=5.0, seed=4, percall_max=2000)
+        sweep = []
+        for rate in (50000.0, 100000.0, 200000.0, 500000.0):
+            # offered for at most 3 s and 150,000 requests; the loop drains what it admitted
+            secs = min(3.0, 150000.0 / rate)
+            r = srv.loadtest(rate=rate, seconds=secs, seed=4, percall_max=0)
+            sweep.append(serve_row(rate, secs, r))
+        poisson = srv.loadtest(rate=50000.0, seconds=args.serve_hold, seed=4, percall_max=2000)
         sat = srv.loadtest(rate=0.0, count=20000, seed=5, percall_max=0)
     finally:
         srv.close()
     ps, ss = poisson["served"], sat["served"]
-    return {"workload": "Poisson 50k req/s x 5 s; c2c/r2c N 64..65536, 2-D 256..1024 per side, fast FIR 255..4095 "
+    return {"workload": "Poisson arrivals; c2c/r2c N 64..65536, 2-D 256..1024 per side, fast FIR 255..4095 "
                         "taps on 2^16..2^22 samples, equal shares, float32, pinned host buffers; seed 4; "
                         "HBM budget 40 GB",
-            "offered": poisson["offered"], "completed": ps["completed"], "failed": ps["failed"],
-            "p50_ms": round(ps["p50_s"] * 1e3, 3), "p99_ms": round(ps["p99_s"] * 1e3, 3),
-            "req_per_s": round(ps["req_per_s"], 1), "gbs": round(ps["gbs"], 2), "batches": ps["batches"],
-            "host_busy_s": round(ps["host_s"], 3),
-            "peak_hbm_gb": round(ps["peak_hbm_bytes"] / 1e9, 3),
+            "held": dict(serve_row(50000.0, args.serve_hold, poisson), batches=ps["batches"],
+                         peak_hbm_gb=round(ps["peak_hbm_bytes"] / 1e9, 3)),
+            "sweep": sweep,
             "saturated": {"requests": sat["offered"], "req_per_s": round(ss["req_per_s"], 1),
                           "gbs": round(ss["gbs"], 2), "p50_ms": round(ss["p50_s"] * 1e3, 3),
                           "p99_ms": round(ss["p99_s"] * 1e3, 3), "host_busy_s": round(ss["host_s"], 3)},
@@ -650,6 +664,62 @@ def run_serving(args):
                         "gbs": round(poisson["percall_gbs"], 2), "p50_ms": round(poisson["percall_p50_s"] * 1e3, 3),
                         "p99_ms": round(poisson["percall_p99_s"] * 1e3, 3)},
             "saturated_vs_percall": round(ss["req_per_s"] / max(poisson["percall_req_per_s"], 1e-9), 2)}
+
+
+def serve_row(rate, secs, r):
+    """One offered rate of the serving loop: latency, what completed, host
+    time, host-link bytes."""
+    sv = r["served"]
+    return {"offered_req_per_s": rate, "seconds": round(secs, 3), "offered": r["offered"],
+            "completed": sv["completed"], "failed": sv["failed"], "req_per_s": round(sv["req_per_s"], 1),
+            "p50_ms": round(sv["p50_s"] * 1e3, 3), "p99_ms": round(sv["p99_s"] * 1e3, 3),
+            "link_gbs": round(sv["gbs"], 2), "host_busy_s": round(sv["host_s"], 3)}
+
+
+def link_peak(mib=512, reps=3):
+    """Measured copy-engine bandwidth of the host link on page-locked
+    buffers (cudaMemcpyAsync through torch copies, CUDA events, best of
+    reps): host to device, device to host, and both at once on two streams
+    (GB/s of bytes moved)."""
+    import torch
+    nb = mib << 20
+    h1 = torch.empty(nb, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nb, dtype=torch.uint8).pin_memory()
+    d1 = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def best(fn):
+        b = None
+        for _ in range(reps + 1):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            b = ms if b is None else min(b, ms)
+        return b
+
+    def both():
+        ev = torch.cuda.Event()
+        ev.record()
+        for st, f in ((s1, lambda: d1.copy_(h1, non_blocking=True)), (s2, lambda: h2.copy_(d2, non_blocking=True))):
+            st.wait_event(ev)
+            with torch.cuda.stream(st):
+                f()
+        cur = torch.cuda.current_stream()
+        cur.wait_stream(s1)
+        cur.wait_stream(s2)
+
+    t_h2d = best(lambda: d1.copy_(h1, non_blocking=True))
+    t_d2h = best(lambda: h2.copy_(d2, non_blocking=True))
+    t_bi = best(both)
+    del h1, h2, d1, d2
+    return {"h2d_gbs": round(nb / (t_h2d * 1e-3) / 1e9, 1), "d2h_gbs": round(nb / (t_d2h * 1e-3) / 1e9, 1),
+            "bidir_gbs": round(2 * nb / (t_bi * 1e-3) / 1e9, 1),
+            "how": "cudaMemcpyAsync of %d MiB page-locked buffers, CUDA events, best of %d" % (mib, reps)}
 
 
 def percall_single(L, st, n=1024, calls=5000):
@@ -747,6 +817,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mix", action="store_true", help="skip the batched uneven-mix measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serve-hold", type=float, default=60.0,
+                    help="seconds the serving loop is held at 50,000 requests/s")
     ap.add_argument("--no-configs", action="store_true", help="skip the real / N-D / round-trip workloads")
     ap.add_argument("--only", choices=["mix", "serve", "configs", "mix-runs", "serve-burst"], default=None,
                     help="run only the uneven-mix or the serving measurement and print it")

@@ -64,6 +64,7 @@ kf.prepare = lambda c, b: None
 kf.kiss_fft_batch = batch
 
 import bench
+bench.link_peak = lambda *a, **k: {"h2d_gbs": 1.0, "d2h_gbs": 1.0, "bidir_gbs": 2.0, "how": "stand-in"}
 bench._CASES = [("float", 480, 32), ("int16_t", 1000, 16), ("int32_t", 3003, 8), ("float", 65536, 2)]
 args = types.SimpleNamespace(steps=2, warmup=3, specialize=1, autotune=1, no_e2e=False, no_cpu=False, no_mix=True,
                              no_serve=True, no_configs=True, cpu_seconds=0.2, traffic=None, case=[])
@@ -95,6 +96,7 @@ def test_gpu_arm_runs_through_on_cpu_stand_ins():
             assert a["bit_exact"]
     assert run["cpu"]["value"] > 0 and run["cpu"]["openmp_build"]["value"] > 0
     assert run["e2e"]["h2d_bytes_per_step"] > 0 and run["e2e"]["d2h_bytes_per_step"] > 0
+    assert run["e2e"]["link"]["bidir_gbs"] > 0 and run["e2e"]["link"]["frac"] > 0
     assert run["roofline"]["bound"] == "hbm" and run["roofline"]["peak"] > 0
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
               "vs_baseline", "dtype", "data", "config", "roofline", "cpu_baseline", "e2e", "clocks", "gpu_launches",
