@@ -85,6 +85,9 @@ struct KTab {
 // (g_hi, g_lo) = (jg / G_lo, jg % G_lo); its input base is
 // g_hi*in_dhi + g_lo*in_dlo and element A sits at base + A*in_stride
 // (units: complex elements, or real samples for the real-input modes).
+// With G_mid > 1, g_hi splits once more into (g_hi / G_mid, g_hi % G_mid),
+// the second part weighted by in_dmid / out_dmid (the strided fibers of an
+// N-D axis that runs as two HBM passes).
 struct KArgs {
     KSub sub[2];              // sub[1]: inverse plan of the fast FIR
     KTab tab[2];
@@ -92,6 +95,7 @@ struct KArgs {
     void* out;
     const void* fir_H;        // fast FIR frequency response (nfft/2+1 bins)
     long long G, G_lo;
+    long long G_mid, in_dmid, out_dmid;  // third level of the job index (G_mid <= 1: none)
     long long in_dhi, in_dlo, in_stride;
     long long out_dhi, out_dlo, out_stride;
     long long in_limit;       // fast FIR: signal length (zero padding beyond)

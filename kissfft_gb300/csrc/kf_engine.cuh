@@ -892,9 +892,13 @@ KF_HD void job_entry(const KArgs& a, long long tile, int J, int j, long long& in
         lin = lout = 0;
         return;
     }
-    long long ghi = jg / a.G_lo, glo = jg - ghi * a.G_lo;
-    inb = (a.in_off ? a.in_off[ghi] : ghi * a.in_dhi) + glo * a.in_dlo;
-    outb = (a.out_off ? a.out_off[ghi] : ghi * a.out_dhi) + glo * a.out_dlo;
+    long long ghi = jg / a.G_lo, glo = jg - ghi * a.G_lo, gmid = 0;
+    if (a.G_mid > 1) {
+        gmid = ghi % a.G_mid;
+        ghi /= a.G_mid;
+    }
+    inb = (a.in_off ? a.in_off[ghi] : ghi * a.in_dhi) + gmid * a.in_dmid + glo * a.in_dlo;
+    outb = (a.out_off ? a.out_off[ghi] : ghi * a.out_dhi) + gmid * a.out_dmid + glo * a.out_dlo;
     U = a.use_u ? (int)glo : 0;
     lin = a.in_limit - inb;
     lout = a.out_limit - outb;

@@ -320,6 +320,7 @@ int build_schedule(kfg_plan* p, long long batch, long long in_dist, long long in
                 if (!schedule_axis(p->axes[k]->p, p->dims.data(), nd, k, batch, k == 0 ? 0 : 1, 1, a))
                     return fail(KFG_EINVAL, a.error);
                 for (auto& st : a.steps) s.steps.push_back(st);
+                s.scratch[0] = std::max(s.scratch[0], a.scratch[0]);  // two-pass axes, one after the other
             }
             in_bytes = out_bytes = (size_t)(batch * tot) * esz;
             return KFG_OK;
@@ -341,6 +342,8 @@ int build_schedule(kfg_plan* p, long long batch, long long in_dist, long long in
                     if (!schedule_axis(p->axes[k]->p, bd.data(), nd, k, batch, 1, 1, a))
                         return fail(KFG_EINVAL, a.error);
                     for (auto& st : a.steps) s.steps.push_back(st);
+                    // the real rows' scratch is free again once the axes run
+                    s.scratch[0] = std::max(s.scratch[0], a.scratch[0]);
                 }
                 in_bytes = (size_t)(batch * other * dr) * rsz;
                 out_bytes = (size_t)(batch * other * nb) * esz;
@@ -348,17 +351,23 @@ int build_schedule(kfg_plan* p, long long batch, long long in_dist, long long in
                 if (nd == 1) {
                     if (!schedule_c2r(p->main->p, batch, nb, dr, s)) return fail(KFG_EINVAL, s.error);
                 } else {
-                    if (p->main->p.nsub != 1) return fail(KFG_EUNSUPPORTED, "N-D real inverse: last axis too long");
+                    size_t tmp = 0;
                     for (int k = 0; k < nd - 1; ++k) {
                         Schedule a;
-                        if (!schedule_axis(p->axes[k]->p, bd.data(), nd, k, batch, k == 0 ? 0 : 2, 2, a))
+                        // the half spectrum lives in role 2; a two-pass axis keeps its intermediate in role 3
+                        if (!schedule_axis(p->axes[k]->p, bd.data(), nd, k, batch, k == 0 ? 0 : 2, 2, a, 3))
                             return fail(KFG_EINVAL, a.error);
                         for (auto& st : a.steps) s.steps.push_back(st);
+                        tmp = std::max(tmp, a.scratch[1]);
                     }
                     Schedule c;
                     if (!schedule_c2r(p->main->p, batch * other, nb, dr, c, 2, 1)) return fail(KFG_EINVAL, c.error);
                     for (auto& st : c.steps) s.steps.push_back(st);
-                    s.scratch[0] = (size_t)(batch * other * nb) * esz;
+                    // role 2: the half spectrum, then (two-pass last axis) the
+                    // c2r's own intermediate once its merge has read it;
+                    // role 3: two-pass axis intermediates, then the merged rows
+                    s.scratch[0] = std::max((size_t)(batch * other * nb) * esz, c.scratch[0]);
+                    s.scratch[1] = std::max(tmp, c.scratch[1]);
                 }
                 in_bytes = (size_t)(batch * other * nb) * esz;
                 out_bytes = (size_t)(batch * other * dr) * rsz;
@@ -616,10 +625,6 @@ kfg_plan* kfg_plan_nd(int dtype, const int* dims, int ndims, int inverse) {
         p->n *= dims[i];
         p->axes.push_back(make_devplan(dtype, dims[i], p->inverse, 0));
         if (!p->axes.back()) return nullptr;
-        if (p->axes.back()->p.nsub != 1) {
-            fail(KFG_EUNSUPPORTED, "kfg_plan_nd: an axis longer than one shared-memory tile");
-            return nullptr;
-        }
     }
     return p.release();
 }
@@ -647,10 +652,6 @@ kfg_plan* kfg_plan_ndr(int dtype, const int* dims, int ndims, int inverse) {
     for (int i = 0; i < ndims - 1; ++i) {
         p->axes.push_back(make_devplan(dtype, dims[i], p->inverse, 0));
         if (!p->axes.back()) return nullptr;
-        if (p->axes.back()->p.nsub != 1) {
-            fail(KFG_EUNSUPPORTED, "kfg_plan_ndr: an axis longer than one shared-memory tile");
-            return nullptr;
-        }
     }
     return p.release();
 }

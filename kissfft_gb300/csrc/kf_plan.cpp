@@ -298,7 +298,8 @@ bool tma_enabled() {
 bool enable_tma(Step& st, const void* in) {
     const KArgs& a = st.args;
     if (!tma_enabled() || !st.tma_ok || st.kind != 0 || (st.mode != MODE_C2C && st.mode != MODE_R2C)) return false;
-    if (a.col_in || a.col_out || a.in_stride != 1 || a.in_dlo != 0 || a.G_lo != 1 || a.in_off) return false;
+    if (a.col_in || a.col_out || a.in_stride != 1 || a.in_dlo != 0 || a.G_lo != 1 || a.G_mid > 1 || a.in_off)
+        return false;
     const long long L = a.sub[0].L, esz = cpx_size(st.dtype);
     if (a.in_dhi != L || (L * esz) % 16 != 0 || ((uintptr_t)in & 15) != 0) return false;
     const long long stage_off = ((long long)st.cfg.smem + 15) / 16 * 16;
@@ -570,17 +571,70 @@ bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long o
 }
 
 bool schedule_axis(const Plan& p, const int* dims, int ndims, int axis, long long batch, int in_role, int out_role,
-                   Schedule& s) {
+                   Schedule& s, int tmp_role) {
     s.steps.clear();
     s.scratch[0] = s.scratch[1] = 0;
-    if (p.nsub != 1) {
-        s.error = "N-D axis longer than one tile is not supported";
-        return false;
-    }
     long long S = 1, outer = batch;
     for (int i = axis + 1; i < ndims; ++i) S *= dims[i];
     for (int i = 0; i < axis; ++i) outer *= dims[i];
     const long long n = dims[axis];
+    if (p.nsub != 1) {
+        // An axis longer than one tile: its fibers (outer o, offset s; element
+        // m at o*n*S + m*S + s) run as the two HBM passes of schedule_c2c.
+        // Pass 1, job (o, s, j < Ps): elements j + k*Ps of the fiber, written
+        // to the intermediate with every fiber contiguous (o*n*S + s*n + m);
+        // pass 2, job (o, s, j < LA): intermediate elements j*Ps + k, written
+        // back to positions j + k*LA of the fiber.
+        if (tmp_role != 2 && tmp_role != 3) {
+            s.error = "N-D axis: bad intermediate buffer";
+            return false;
+        }
+        const long long Ps = p.sub[1].L, LA = p.sub[0].L;
+        const int esz = cpx_size(p.dtype);
+        Step a;
+        a.mode = MODE_C2C;
+        a.dtype = p.dtype;
+        a.args = base_args(p, 0);
+        set_shape(a, p, 0);
+        a.args.G = outer * S * Ps;
+        a.args.G_lo = Ps;
+        a.args.G_mid = S;
+        a.args.in_dhi = n * S;
+        a.args.in_dmid = 1;
+        a.args.in_dlo = S;
+        a.args.in_stride = Ps * S;
+        a.args.out_dhi = n * S;
+        a.args.out_dmid = n;
+        a.args.out_dlo = 1;
+        a.args.out_stride = Ps;
+        a.in_role = in_role;
+        a.out_role = tmp_role;
+        finish(a, default_cfg(p.sub[0], p.dtype, MODE_C2C, a.args.G, 1, 1));
+        Step b;
+        b.mode = MODE_C2C;
+        b.dtype = p.dtype;
+        b.args = base_args(p, 1);
+        set_shape(b, p, 1);
+        b.args.G = outer * S * LA;
+        b.args.G_lo = LA;
+        b.args.G_mid = S;
+        b.args.in_dhi = n * S;
+        b.args.in_dmid = n;
+        b.args.in_dlo = Ps;
+        b.args.in_stride = 1;
+        b.args.out_dhi = n * S;
+        b.args.out_dmid = 1;
+        b.args.out_dlo = S;
+        b.args.out_stride = LA * S;
+        b.args.use_u = 1;
+        b.in_role = tmp_role;
+        b.out_role = out_role;
+        finish(b, default_cfg(p.sub[1], p.dtype, MODE_C2C, b.args.G, 0, 1));
+        s.steps.push_back(a);
+        s.steps.push_back(b);
+        s.scratch[tmp_role - 2] = (size_t)(outer * S * n) * esz;
+        return fits(s);
+    }
     Step st;
     st.mode = MODE_C2C;
     st.dtype = p.dtype;

@@ -126,9 +126,10 @@ bool schedule_r2c(const Plan& p, long long batch, long long in_dist, long long o
 bool schedule_c2r(const Plan& p, long long batch, long long in_dist, long long out_dist, Schedule& s,
                   int in_role = 0, int out_role = 1);
 // Complex transform of every fiber along `axis` of a row-major array of
-// `batch` arrays with shape dims (plan length = dims[axis]).
+// `batch` arrays with shape dims (plan length = dims[axis]).  A two-pass
+// axis plan keeps its intermediate in scratch role tmp_role (2 or 3).
 bool schedule_axis(const Plan& p, const int* dims, int ndims, int axis, long long batch, int in_role, int out_role,
-                   Schedule& s);
+                   Schedule& s, int tmp_role = 2);
 // Real overlap-scrap FIR of a signal of Ns samples with fw/iv real plans
 // of nfft and filter response H (bound to a device pointer by the caller).
 bool schedule_fastfir(const Plan& fw, const Plan& iv, long long L, long long Ns, long long nblocks_first,

@@ -258,7 +258,22 @@ int emu_c2r(int dtype, int nfft, int lmax, const void* in, void* out, long long 
     return run_schedule(s, in, out);
 }
 
-// In-place complex transform along one axis of a row-major array.
+// In-place complex transform along one axis of a row-major array; lmax
+// caps the tile length (0: the dtype's default), so small axes can take the
+// two-pass route.
+int emu_axis_lmax(int dtype, const int* dims, int ndims, int axis, int inverse, int lmax, void* buf) {
+    Plan p;
+    if (!p.build(dtype, dims[axis], inverse, lmax)) return -2;
+    p.bind(p.blob.data());
+    Schedule s;
+    if (!schedule_axis(p, dims, ndims, axis, 1, 0, 1, s)) return -3;
+    long long total = 1;
+    for (int i = 0; i < ndims; ++i) total *= dims[i];
+    EmuOwn own_p(p.blob.data(), p.blob.size());
+    EmuOwn own_b(buf, (size_t)(total * cpx_size(dtype)));
+    return run_schedule(s, buf, buf);
+}
+
 int emu_axis(int dtype, const int* dims, int ndims, int axis, int inverse, void* buf) {
     Plan p;
     if (!p.build(dtype, dims[axis], inverse)) return -2;

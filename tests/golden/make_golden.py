@@ -38,8 +38,11 @@ DTYPES = ["float", "double", "int16_t", "int32_t"]
 C2C_SIZES = [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 16, 25, 30, 32, 49, 64, 97, 112, 120, 121, 136, 169, 257, 480,
              961, 1000, 1024, 2048, 3003, 4096, 4099, 16384, 17017, 34034, 65536, 131072]
 R_SIZES = [2, 4, 6, 8, 10, 12, 30, 64, 120, 480, 1000, 2048, 4096, 6006, 34034]
-ND_DIMS = [[2, 3], [4, 4], [3, 5, 7], [8, 6], [2, 3, 4, 6], [16, 32], [64, 64], [5, 7, 11], [128, 96]]
-NDR_DIMS = [[2, 4], [4, 4], [3, 5, 8], [8, 6], [2, 3, 4, 6], [16, 32], [32, 64], [8, 16, 16], [6, 10]]
+ND_DIMS = [[2, 3], [4, 4], [3, 5, 7], [8, 6], [2, 3, 4, 6], [16, 32], [64, 64], [5, 7, 11], [128, 96],
+           # axes longer than one shared-memory tile (two HBM passes on the GPU)
+           [32768, 3], [2, 65536], [3, 40000, 2]]
+NDR_DIMS = [[2, 4], [4, 4], [3, 5, 8], [8, 6], [2, 3, 4, 6], [16, 32], [32, 64], [8, 16, 16], [6, 10],
+            [40000, 4], [3, 65536]]
 TW_SIZES = [480, 1000, 1024, 2048, 3003, 4096, 17017, 65536, 131072]
 FIR_CASES = [(255, 20000), (1000, 50000), (4095, 70000), (17, 5000)]
 SMALL = 64
