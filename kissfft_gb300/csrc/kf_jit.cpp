@@ -58,9 +58,11 @@ unsigned long long fnv1a(const std::string& s, unsigned long long h = 1469598103
     return h;
 }
 
+// Digest of the embedded headers (part of every cache key).  A function
+// static initialised once (thread-safe): the autotuner's first compiles run
+// on several threads at once.
 std::string headers_digest() {
-    static std::string d;
-    if (d.empty()) {
+    static const std::string d = [] {
         unsigned long long h = 1469598103934665603ull;
         for (int i = 0; i < kf_hdr_count; ++i) {
             h = fnv1a(kf_hdr_names[i], h);
@@ -68,8 +70,8 @@ std::string headers_digest() {
         }
         char buf[32];
         snprintf(buf, sizeof(buf), "%016llx", h);
-        d = buf;
-    }
+        return std::string(buf);
+    }();
     return d;
 }
 

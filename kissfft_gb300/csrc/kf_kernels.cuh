@@ -23,13 +23,12 @@ unsigned long long current_context_id();
 inline long long launch_grid(const void* k, const Step& st) {
     long long grid = st.cfg.grid;
     if (st.args.tma) {
-        static int nsm = 0;
-        if (!nsm) {
-            int dev = 0;
+        static const int nsm = [] {
+            int dev = 0, n = 0;
             cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            if (nsm <= 0) nsm = 1;
-        }
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            return n > 0 ? n : 1;
+        }();
         // occupancy of the last (kernel, threads, shared memory) this thread asked for
         thread_local const void* ck = nullptr;
         thread_local int cT = 0, cS = 0, cper = 1;
