@@ -88,8 +88,10 @@ struct KTab {
 // With G_mid > 1, g_hi splits once more into (g_hi / G_mid, g_hi % G_mid),
 // the second part weighted by in_dmid / out_dmid (the strided fibers of an
 // N-D axis that runs as two HBM passes).
-struct KArgs {
-    KSub sub[2];              // sub[1]: inverse plan of the fast FIR
+// KRun holds everything but the plan shape: the argument of the
+// plan-specialised kernels (whose shape is a compile-time constant), a few
+// hundred bytes per launch instead of the shapes' kilobytes.
+struct KRun {
     KTab tab[2];
     const void* in;
     void* out;
@@ -112,6 +114,12 @@ struct KArgs {
     int stage_off;            // byte offset of the staging buffer in dynamic shared memory
     int swz;                  // shared-tile layout: SWZ_FOLD, SWZ_NONE or SWZ_ONE (kf_engine.cuh swz)
     int* err;                 // device error word: bit 0 bad pass kind, bit 1 TMA wait timeout
+};
+
+// A launch's full arguments: the run-time part and the sub-plan shapes that
+// the precompiled kernels read at run time (sub[1]: inverse plan of the fast FIR).
+struct KArgs : KRun {
+    KSub sub[2];
 };
 
 // A persistent multi-plan launch: CTAs take work items (a step's tile) from

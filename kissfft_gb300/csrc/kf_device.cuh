@@ -50,7 +50,7 @@ struct DevExec {
     // has read it (next >= 0: the tile to fetch)
     long long next = -1;
     unsigned bar = 0, stage = 0;
-    const KArgs* args = nullptr;
+    const KRun* args = nullptr;
     int L = 0;
     __device__ void input_consumed() {
         if (next >= 0 && threadIdx.x == 0) {
@@ -95,7 +95,7 @@ struct DevExec {
 // tile lives in dynamic shared memory.  JF/CIF/COF > 0 fix the tile shape at
 // compile time (specialised kernels); 0 takes it from the arguments.
 template <typename S, int MODE, kmask_t KM, int JF = 0, int CIF = -1, int COF = -1, int SWF = -1>
-__device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, const KSub& s1) {
+__device__ __forceinline__ void engine_body(const KRun& a, const KSub& s0, const KSub& s1) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
     __shared__ int s_U[KF_MAXJ];
@@ -127,7 +127,7 @@ __device__ __forceinline__ void engine_body(const KArgs& a, const KSub& s0, cons
 // is bulk-copied into a staging buffer while the current tile runs its
 // passes; the first pass reads the staged tile through shared memory.
 template <typename S, int MODE, kmask_t KM, int JF = 0, int SWF = -1>
-__device__ __forceinline__ void engine_body_tma(const KArgs& a, const KSub& s0) {
+__device__ __forceinline__ void engine_body_tma(const KRun& a, const KSub& s0) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
     __shared__ int s_U[KF_MAXJ];
@@ -192,23 +192,40 @@ __global__ void __launch_bounds__(KF_MAXT) kf_engine_kernel(const __grid_constan
 }
 
 // Persistent multi-plan kernel: tiles of many plans (one sample type and
-// mode) in one launch, pulled from a work queue.  Every step's shape is read
-// from its KArgs in global memory; blockDim and the shared tile are sized
-// for the largest step of the launch.
+// mode) in one launch, pulled from a work queue.  Every step carries its own
+// shape (KArgs in global memory); the CTA copies the step's KArgs into shared
+// memory when it takes an item, so the passes read the shape with shared
+// loads instead of global ones on their address paths.  blockDim and the
+// shared tile are sized for the largest step of the launch.
+// Registers capped at 80 a thread (up to 512 threads a block): every pass
+// kind of a family is compiled in, and without a cap the compiler takes 128
+// and leaves the work-queue launches at a quarter of the warps; 80 was the
+// fastest of 64/80/96/128 on the uneven mix.
 template <typename S, int MODE, kmask_t KM>
-__global__ void __launch_bounds__(KF_MAXT) kf_multi_kernel(const __grid_constant__ MultiArgs m) {
+__global__ void __maxnreg__(80) kf_multi_kernel(const __grid_constant__ MultiArgs m) {
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
     __shared__ int s_U[KF_MAXJ];
     __shared__ unsigned long long s_item;
+    __shared__ __align__(16) KArgs s_args;
+    static_assert(sizeof(KArgs) % 8 == 0, "KArgs copies as 8-byte words");
     DevExec<S, MODE, KM> x;
+    int cur = -1;  // step whose arguments s_args holds (the same in every thread)
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(m.counter, 1ull);
         __syncthreads();
         const unsigned long long it = s_item;
         if (it >= (unsigned long long)m.nitems) break;
         const MultiItem w = m.items[it];
-        const KArgs& a = m.steps[w.step];
+        if (w.step != cur) {
+            // every thread is past the previous tile (barrier at its end)
+            const uint2* src = (const uint2*)(m.steps + w.step);
+            uint2* dst = (uint2*)&s_args;
+            for (int k = threadIdx.x; k < (int)(sizeof(KArgs) / 8); k += blockDim.x) dst[k] = src[k];
+            cur = w.step;
+            __syncthreads();
+        }
+        const KArgs& a = s_args;
         Tile<S> t;
         tile_layout(a, a.sub[0].L, a.J, a.logJ, a.col_in | a.col_out, t);
         t.sm = (cpx<S>*)kf_dyn_smem;

@@ -882,7 +882,7 @@ KF_HD void merge_item(const KArgs& a, long long it) {
 }
 
 // Job table entries for tile slot j (any thread may fill one).
-KF_HD void job_entry(const KArgs& a, long long tile, int J, int j, long long& inb, long long& outb, int& U,
+KF_HD void job_entry(const KRun& a, long long tile, int J, int j, long long& inb, long long& outb, int& U,
                      long long& lin, long long& lout) {
     long long jg = tile * J + j;
     if (jg >= a.G) {

@@ -138,7 +138,8 @@ bool spec_compile_only(const Step& st, std::string& err);
 inline cudaError_t launch_spec(const void* k, const Step& st, cudaStream_t s) {
     const long long grid = launch_grid(k, st);
     if (grid <= 0) return cudaSuccess;
-    void* args[] = {(void*)&st.args};
+    // the specialised kernels take the run-time part only (their shape is compiled in)
+    void* args[] = {(void*)static_cast<const KRun*>(&st.args)};
     return cudaLaunchKernel(k, dim3((unsigned)grid), dim3(st.cfg.T), args, (size_t)st.cfg.smem, s);
 }
 

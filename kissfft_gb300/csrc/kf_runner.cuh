@@ -42,7 +42,7 @@ KF_HD void run_sub(X& x, Tile<S>& t, const KSub& sb, const KTab& tb, bool src_fi
 #pragma nv_exec_check_disable
 #endif
 template <typename S, int MODE, kmask_t KM, class X>
-KF_HD void run_tile(X& x, const KArgs& a, const KSub& s0, const KSub& s1, Tile<S>& t, int ci, int co) {
+KF_HD void run_tile(X& x, const KRun& a, const KSub& s0, const KSub& s1, Tile<S>& t, int ci, int co) {
     if constexpr (MODE == MODE_C2R) {
         t.col = ci;
         x.c2r_pre(t, s0, a.tab[0]);
@@ -64,7 +64,7 @@ KF_HD void run_tile(X& x, const KArgs& a, const KSub& s0, const KSub& s1, Tile<S
 // Shared-memory layout of a tile: interleaved jobs (column launches) or
 // job-major rows.
 template <typename S>
-KF_HD void tile_layout(const KArgs& a, int L, int J, int logJ, int col, Tile<S>& t) {
+KF_HD void tile_layout(const KRun& a, int L, int J, int logJ, int col, Tile<S>& t) {
     t.J = J;
     t.logJ = logJ;
     if (col) {

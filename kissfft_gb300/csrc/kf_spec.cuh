@@ -18,7 +18,7 @@ __device__ constexpr ShapeInfo kSpecShape = make_shape(DT, N, INV, LMAX, 0);
 // SM bound the registers a thread.
 template <typename S, int MODE, int DT, int N, int INV, int LMAX, int SUB, int J, int COLIN, int COLOUT, int T,
           int MINB, int SWZ>
-__global__ void __launch_bounds__(T, MINB) kf_spec_kernel(const __grid_constant__ KArgs a) {
+__global__ void __launch_bounds__(T, MINB) kf_spec_kernel(const __grid_constant__ KRun a) {
     static_assert(kSpecShape<DT, N, INV, LMAX>.error == 0, "plan shape");
     constexpr kmask_t KM = kind_mask(kSpecShape<DT, N, INV, LMAX>.sub[SUB]);
     if constexpr ((MODE == MODE_C2C || MODE == MODE_R2C) && COLIN == 0 && COLOUT == 0) {
