@@ -727,29 +727,42 @@ def link_peak(mib=512, reps=3):
 def percall_single(L, st, n=1024, calls=5000):
     """Host cost of one plain drop-in call: a 1024-point float forward
     transform on device buffers (kfg_exec, enqueued on the stream), timed
-    over `calls` back-to-back calls from Python (ctypes), with the cost of a
-    ctypes call that does nothing beside it."""
+    over `calls` back-to-back calls from Python (ctypes), with the
+    plan-specialised kernels and with the precompiled family kernels, and
+    the cost of a ctypes call that does nothing beside them."""
     import ctypes
     import torch
+
+    import kissfft_gb300 as kf
     vp = ctypes.c_void_p
     p = L.kfg_plan_c2c(0, n, 0)
     x = torch.randn(2 * n, device="cuda")
     y = torch.empty_like(x)
     xa, ya = vp(x.data_ptr()), vp(y.data_ptr())
-    for _ in range(50):
-        L.kfg_exec(p, xa, ya, st)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(calls):
-        L.kfg_exec(p, xa, ya, st)
+
+    def per_call(spec):
+        kf.set_specialize(spec)
+        for _ in range(200):
+            L.kfg_exec(p, xa, ya, st)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            L.kfg_exec(p, xa, ya, st)
+        t1 = time.perf_counter()
+        torch.cuda.synchronize()
+        return (t1 - t0) / calls * 1e6
+
+    us_spec = per_call(True)
+    us_fam = per_call(False)
     t1 = time.perf_counter()
-    torch.cuda.synchronize()
     for _ in range(calls):
         L.kfg_get_stream()
     t2 = time.perf_counter()
     L.kfg_plan_free(p)
-    return {"nfft": n, "us": round((t1 - t0) / calls * 1e6, 2), "python_ctypes_us": round((t2 - t1) / calls * 1e6, 2),
-            "calls": calls, "what": "kfg_exec on device buffers, host time per call including the Python call"}
+    return {"nfft": n, "us": round(us_spec, 2), "us_precompiled": round(us_fam, 2),
+            "python_ctypes_us": round((t2 - t1) / calls * 1e6, 2), "calls": calls,
+            "what": "kfg_exec on device buffers, host time per call including the Python call; us: plan-specialised "
+                    "kernels, us_precompiled: the precompiled family kernels"}
 
 
 # ------------------------------------------------------------------ CPU arm
