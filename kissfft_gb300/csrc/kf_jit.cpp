@@ -127,16 +127,8 @@ bool compile(const std::string& name, std::string& cubin, std::string& lowered, 
     }
     std::string expr = "&" + name;
     nvrtcAddNameExpression(prog, expr.c_str());
-    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true"};
-    // EXPERIMENT (to be removed): extra -D options for variant timing
-    std::vector<std::string> xdefs;
-    if (const char* e = getenv("KISSFFT_GB300_JIT_DEFS")) {
-        std::istringstream is(e);
-        std::string d;
-        while (is >> d) xdefs.push_back(d);
-    }
-    for (auto& d : xdefs) opts.push_back(d.c_str());
-    nvrtcResult r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true"};
+    nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
     if (r != NVRTC_SUCCESS) {
         size_t n = 0;
         nvrtcGetProgramLogSize(prog, &n);
@@ -205,8 +197,7 @@ const void* spec_kernel(const Step& st, std::string& err) {
     nvrtcVersion(&ver[0], &ver[1]);
     char key[64];
     snprintf(key, sizeof(key), "%016llx",
-             fnv1a(name + "|" + headers_digest() + "|sm_103a|" + std::to_string(ver[0] * 100 + ver[1]) + "|" +
-                   (getenv("KISSFFT_GB300_JIT_DEFS") ? getenv("KISSFFT_GB300_JIT_DEFS") : "")));
+             fnv1a(name + "|" + headers_digest() + "|sm_103a|" + std::to_string(ver[0] * 100 + ver[1])));
     const std::string dir = cache_dir();
     const std::string cpath = dir + "/" + key + ".cubin", npath = dir + "/" + key + ".name";
     std::string cubin, lowered;

@@ -1366,14 +1366,12 @@ int batch_commit(kfg_batch* b) {
         }
     }
     // launches: engine tiles keyed by (phase, dtype, mode, family, threads
-    // class, shared-memory class), so that small tiles are not run with the
-    // block shape of the largest; split / merge elements keyed by (phase,
-    // dtype, kind)
-    auto pow2_ceil = [](long long v) {
-        long long c = 1;
-        while (c < v) c <<= 1;
-        return c;
-    };
+    // class, shared-memory class) -- two classes each (up to 256 threads or
+    // more; up to 64 KiB of tile or more), so that small tiles do not run
+    // with the block shape of the largest (on the 20,000-request mix: 44
+    // launches in 4.96 ms; one class each, 16 launches, took 5.80 ms and one
+    // class per power of two, 108 launches, 5.14 ms); split / merge elements
+    // keyed by (phase, dtype, kind)
     std::map<std::string, int> lkey;
     for (size_t i = 0; i < b->steps.size(); ++i) {
         const Step& st = b->steps[i];
@@ -1381,8 +1379,8 @@ int batch_commit(kfg_batch* b) {
         if (st.kind != 0)
             k << "E" << phase_of[i] << ":" << st.dtype << ":" << st.kind;
         else
-            k << phase_of[i] << ":" << st.dtype << ":" << st.mode << ":" << st.fam << ":" << pow2_ceil(st.cfg.T) << ":"
-              << pow2_ceil(std::max(st.cfg.smem, 8192));
+            k << phase_of[i] << ":" << st.dtype << ":" << st.mode << ":" << st.fam << ":" << (st.cfg.T > 256) << ":"
+              << (st.cfg.smem > 65536);
         auto it = lkey.find(k.str());
         int li;
         if (it == lkey.end()) {
