@@ -17,6 +17,7 @@
 #include <array>
 #include <atomic>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -1252,11 +1253,14 @@ struct kfg_batch {
         int elem_kind = 0;  // 0: engine tiles; 1 / 2: real split / merge elements
         double cost = 0;
         std::vector<MultiItem> items;
+        std::vector<int> groups;  // plan groups with steps in this launch (sorted)
+        std::vector<int> deps;    // launches of the previous phase that hold steps of those groups
+        cudaEvent_t done = nullptr;
         MultiItem* d_items = nullptr;
         unsigned long long* d_counter = nullptr;
     };
-    // launches of one phase are independent: they run on several streams
-    static constexpr int kAux = 3;
+    // launches run on several streams, each after the launches it depends on
+    static constexpr int kAux = 7;
     cudaStream_t aux[kAux] = {};
     cudaEvent_t fork = nullptr, join[kAux] = {};
     std::vector<Req> reqs;
@@ -1279,6 +1283,8 @@ struct kfg_batch {
         graph = nullptr;
         for (void* p : allocs) cudaFree(p);
         allocs.clear();
+        for (auto& L : launches)
+            if (L.done) cudaEventDestroy(L.done);
         launches.clear();
         steps.clear();
         d_steps = nullptr;
@@ -1321,7 +1327,8 @@ int batch_commit(kfg_batch* b) {
         if (!p) return KFG_EINVAL;
         b->req_plan[i] = p;
     }
-    std::vector<int> phase_of;
+    std::vector<int> phase_of, group_of;
+    int gi = 0;
     for (auto& kv : groups) {
         const auto& idx = kv.second;
         kfg_plan* p = b->req_plan[idx[0]];
@@ -1363,7 +1370,9 @@ int batch_commit(kfg_batch* b) {
             }
             b->steps.push_back(st);
             phase_of.push_back(ph++);
+            group_of.push_back(gi);
         }
+        ++gi;
     }
     // launches: engine tiles keyed by (phase, dtype, mode, family, threads
     // class, shared-memory class) -- two classes each (up to 256 threads or
@@ -1397,6 +1406,7 @@ int batch_commit(kfg_batch* b) {
             li = it->second;
         }
         auto& L = b->launches[li];
+        if (L.groups.empty() || L.groups.back() != group_of[i]) L.groups.push_back(group_of[i]);
         if (st.kind != 0) {
             const long long total = st.args.G * (st.args.sub[0].L / 2 + 1);
             for (long long c = 0; c * KF_ELEM_CHUNK < total; ++c) L.items.push_back(MultiItem{(int)i, 0, c});
@@ -1430,6 +1440,27 @@ int batch_commit(kfg_batch* b) {
     std::stable_sort(b->launches.begin(), b->launches.end(), [](const kfg_batch::Launch& a, const kfg_batch::Launch& c) {
         return a.phase != c.phase ? a.phase < c.phase : a.cost > c.cost;
     });
+    // A launch waits only for the launches of the previous phase that hold
+    // steps of its own plan groups (a plan's steps are one phase apart), not
+    // for the whole previous phase: long single-pass tiles no longer hold
+    // back the second passes of other plans.
+    for (auto& L : b->launches) {
+        std::sort(L.groups.begin(), L.groups.end());
+        L.groups.erase(std::unique(L.groups.begin(), L.groups.end()), L.groups.end());
+    }
+    for (size_t l = 0; l < b->launches.size(); ++l) {
+        auto& L = b->launches[l];
+        if (L.phase == 0) continue;
+        for (size_t m = 0; m < l; ++m) {
+            const auto& M = b->launches[m];
+            if (M.phase != L.phase - 1) continue;
+            std::vector<int> common;
+            std::set_intersection(L.groups.begin(), L.groups.end(), M.groups.begin(), M.groups.end(),
+                                  std::back_inserter(common));
+            if (!common.empty()) L.deps.push_back((int)m);
+        }
+    }
+    for (auto& L : b->launches) KFG_CK(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
     for (int k = 0; k < kfg_batch::kAux; ++k) {
         if (!b->aux[k]) KFG_CK(cudaStreamCreateWithFlags(&b->aux[k], cudaStreamNonBlocking));
         if (!b->join[k]) KFG_CK(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
@@ -1457,26 +1488,30 @@ cudaError_t batch_launch(kfg_batch* b, const kfg_batch::Launch& L, cudaStream_t 
 // Phases run in order on strm; the launches of one phase fork onto the
 // auxiliary streams and join back before the next phase.
 int batch_enqueue(kfg_batch* b, cudaStream_t strm) {
-    size_t i = 0;
-    while (i < b->launches.size()) {
-        size_t j = i;
-        while (j < b->launches.size() && b->launches[j].phase == b->launches[i].phase) ++j;
-        const int naux = (int)std::min<size_t>(j - i - 1, kfg_batch::kAux);
-        if (naux > 0) {
-            KFG_CK(cudaEventRecord(b->fork, strm));
-            for (int k = 0; k < naux; ++k) KFG_CK(cudaStreamWaitEvent(b->aux[k], b->fork, 0));
-        }
-        for (size_t l = i; l < j; ++l) {
-            const int lane = (int)((l - i) % (size_t)(naux + 1));
-            cudaStream_t s = lane == 0 ? strm : b->aux[lane - 1];
-            cudaError_t e = batch_launch(b, b->launches[l], s);
-            if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("kfg_batch launch: ") + cudaGetErrorString(e));
-        }
-        for (int k = 0; k < naux; ++k) {
-            KFG_CK(cudaEventRecord(b->join[k], b->aux[k]));
-            KFG_CK(cudaStreamWaitEvent(strm, b->join[k], 0));
-        }
-        i = j;
+    // lanes: strm and the auxiliary streams; each launch goes to the lane
+    // that frees up first by the launches' estimated costs, after waiting
+    // for the events of the launches it depends on
+    const int nl = 1 + kfg_batch::kAux;
+    std::vector<double> lane_t(nl, 0.0), fin(b->launches.size(), 0.0);
+    KFG_CK(cudaEventRecord(b->fork, strm));
+    for (int k = 0; k < kfg_batch::kAux; ++k) KFG_CK(cudaStreamWaitEvent(b->aux[k], b->fork, 0));
+    for (size_t l = 0; l < b->launches.size(); ++l) {
+        const auto& L = b->launches[l];
+        double ready = 0;
+        for (int d : L.deps) ready = std::max(ready, fin[d]);
+        int best = 0;
+        for (int k = 1; k < nl; ++k)
+            if (std::max(lane_t[k], ready) < std::max(lane_t[best], ready)) best = k;
+        cudaStream_t s = best == 0 ? strm : b->aux[best - 1];
+        for (int d : L.deps) KFG_CK(cudaStreamWaitEvent(s, b->launches[d].done, 0));
+        cudaError_t e = batch_launch(b, L, s);
+        if (e != cudaSuccess) return fail(KFG_ECUDA, std::string("kfg_batch launch: ") + cudaGetErrorString(e));
+        KFG_CK(cudaEventRecord(L.done, s));
+        fin[l] = lane_t[best] = std::max(lane_t[best], ready) + std::max(L.cost, 1.0);
+    }
+    for (int k = 0; k < kfg_batch::kAux; ++k) {
+        KFG_CK(cudaEventRecord(b->join[k], b->aux[k]));
+        KFG_CK(cudaStreamWaitEvent(strm, b->join[k], 0));
     }
     return KFG_OK;
 }
