@@ -544,7 +544,8 @@ def run_configs(args):
     forward+inverse round trip on 4096 transforms (seed 0); kiss_fftr and
     kiss_fftri at nfft 4096 on 65536 rows of 3 unit sinusoids + N(0, 0.1^2)
     noise (generated on the device, seed 2); kiss_fftnd on a 2048x2048
-    complex array; kiss_fftndr / kiss_fftndri on a 128^3 real array.  GB/s of
+    complex array; kiss_fftndr / kiss_fftndri on a 128^3 real array (every
+    plan autotuned and its specialised kernels compiled first).  GB/s of
     compulsory bytes (c2c 2*N*8, r2c 4N + 8(N/2+1), nd 2*prod*8, ndr
     4*prod + 8*prod/N*(N/2+1) per transform)."""
     import torch
@@ -611,12 +612,17 @@ def run_configs(args):
     a = torch.from_numpy(inputs.cpx((2048, 2048), "float", 2).view(np.float32).copy()).to(dev)
     b = torch.empty_like(a)
     nd = kf.kiss_fftnd_alloc([2048, 2048], 0)
+    kf.autotune(nd, 1)
+    kf.prepare(nd, 1)
     out["nd_2048x2048"] = row(2 * 2048 * 2048 * 8, timed(lambda: kf.kiss_fftnd(nd, a, b)), "32 MiB: L2-resident")
     rng = np.random.default_rng(2)
     v = torch.from_numpy(rng.standard_normal((128, 128, 128)).astype(np.float32)).to(dev)
     w = torch.empty((128, 128, 65, 2), device=dev, dtype=torch.float32)
     v2 = torch.empty_like(v)
     ndr, ndri = kf.kiss_fftndr_alloc([128, 128, 128], 0), kf.kiss_fftndr_alloc([128, 128, 128], 1)
+    for c in (ndr, ndri):
+        kf.autotune(c, 1)
+        kf.prepare(c, 1)
     nbytes = 4 * 128 ** 3 + 8 * 128 * 128 * 65
     out["ndr_128^3"] = row(nbytes, timed(lambda: kf.kiss_fftndr(ndr, v, w)), "8 MiB: L2-resident")
     out["ndri_128^3"] = row(nbytes, timed(lambda: kf.kiss_fftndri(ndri, w, v2)), "8 MiB: L2-resident")

@@ -259,6 +259,54 @@ def test_ndr_golden(kf, golden, dtype):
             assert np.linalg.norm(t - ref) / np.linalg.norm(ref) <= 4 * bound(dtype, t.size), c
 
 
+@pytest.mark.parametrize("dtype", ["float", "int16_t"])
+def test_nd_autotuned_and_specialised(kf, dtype):
+    """N-D transforms after the autotuner has picked their launch shapes and
+    with plan-specialised kernels: complex 2-D (one axis longer than a tile),
+    real 3-D forward and inverse, against the oracle (Q15 bit for bit)."""
+    kf.set_specialize(True)
+    try:
+        for dims in ([48, 20000], [24, 40, 16]):
+            x = inputs.cpx(tuple(dims), dtype, 77)
+            cfg = kf.kiss_fftnd_alloc(dims, 0, dtype)
+            kf.autotune(cfg, 1)
+            kf.prepare(cfg, 1)
+            od = empty_dev(x)
+            kf.kiss_fftnd(cfg, to_dev(x), od)
+            y = from_dev(od, x)
+            ref = kfo.fftnd(x, dims, 0, dtype)
+            if fixed(dtype):
+                assert np.array_equal(y, ref), dims
+            else:
+                assert relerr_rows(c128(y, dtype)[None], c128(ref, dtype)[None]) <= bound(dtype, x.size), dims
+            cfg.free()
+        dims = [32, 24, 40]
+        t = inputs.real(tuple(dims), dtype, 78)
+        fcfg, icfg = kf.kiss_fftndr_alloc(dims, 0, dtype), kf.kiss_fftndr_alloc(dims, 1, dtype)
+        for c in (fcfg, icfg):
+            kf.autotune(c, 1)
+            kf.prepare(c, 1)
+        out = kfo.empty_cpx((32, 24, 21), dtype)
+        od = empty_dev(out)
+        kf.kiss_fftndr(fcfg, to_dev(t), od)
+        f = from_dev(od, out)
+        back = np.zeros(tuple(dims), kfo.SCALAR[dtype])
+        bd = empty_dev(back)
+        kf.kiss_fftndri(icfg, to_dev(f), bd)
+        tb = from_dev(bd, back)
+        if fixed(dtype):
+            assert np.array_equal(f, kfo.fftndr(t, dims, dtype))
+            assert np.array_equal(tb, kfo.fftndri(f, dims, dtype))
+        else:
+            assert relerr_rows(c128(f, dtype)[None], c128(kfo.fftndr(t, dims, dtype), dtype)[None]) <= bound(dtype, t.size)
+            ref = kfo.fftndri(f, dims, dtype)
+            assert np.linalg.norm(tb - ref) / np.linalg.norm(ref) <= 4 * bound(dtype, t.size)
+        fcfg.free()
+        icfg.free()
+    finally:
+        kf.set_specialize(False)
+
+
 def test_fastfir_golden(kf, golden):
     for c in golden["fastfir"]:
         rng = np.random.default_rng(c["seed"])
