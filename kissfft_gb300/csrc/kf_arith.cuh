@@ -87,9 +87,9 @@ struct ArIeee {
     static KF_HD W tr(W x) { return x; }
     template <int P>
     static KF_HD CW fixdiv_w(CW c) { return c; }
-    static KF_HD CW cmul_w(CW a, C b) { return cmul(a, b); }
-    static KF_HD W smul_w(W a, S b) { return a * b; }
-    static KF_HD CW mulsc_w(CW c, S s) { return mulsc(c, s); }
+    static KF_HD CW cmul_w(CW a, CW b) { return cmul(a, b); }
+    static KF_HD W smul_w(W a, W b) { return a * b; }
+    static KF_HD CW mulsc_w(CW c, W s) { return mulsc(c, s); }
 };
 
 template <typename S, typename P, int FB, int64_t SMAX>
@@ -224,17 +224,17 @@ struct ArFixed {
         r.i = rnd1(c.i, k);
         return r;
     }
-    // C_MUL(m, a, b), a within the sample range, b a table twiddle; the
-    // result is left untruncated
-    static KF_HD CW cmul_w(CW a, C b) {
+    // C_MUL(m, a, b), a within the sample range, b a table twiddle held as W
+    // (Q15 stage tables store them widened); the result is left untruncated
+    static KF_HD CW cmul_w(CW a, CW b) {
         CW m;
         m.r = rnd_sub(a.r, b.r, a.i, b.i);
         m.i = rnd_add(a.r, b.i, a.i, b.r);
         return m;
     }
     // S_MUL / C_MULBYSCALAR: |a*b| < 2^(2*FB), so the result fits the sample type
-    static KF_HD W smul_w(W a, S b) { return rnd1(a, b); }
-    static KF_HD CW mulsc_w(CW c, S s) {
+    static KF_HD W smul_w(W a, W b) { return rnd1(a, b); }
+    static KF_HD CW mulsc_w(CW c, W s) {
         CW r;
         r.r = rnd1(c.r, s);
         r.i = rnd1(c.i, s);
@@ -354,8 +354,10 @@ KF_HD typename Ar<S>::CW w_sub(typename Ar<S>::CW a, typename Ar<S>::CW b) {
 // constants c0/c1 are epi3 (radix 3) or ya/yb (radix 5).
 
 // kf_bfly2, kiss_fft.c:15-36
+// Twiddles and constants arrive as Ar<S>::CW (the plan tables' entries; for
+// Q15 widened to 32-bit words).
 template <typename S, int VS>
-KF_HD void bfly2(cpx<S>* v, const cpx<S>* w) {
+KF_HD void bfly2(cpx<S>* v, const typename Ar<S>::CW* w) {
     typedef Ar<S> A;
     typedef typename A::CW CW;
     CW a = A::template fixdiv_w<2>(A::widen(v[0])), b = A::template fixdiv_w<2>(A::widen(v[VS]));
@@ -366,7 +368,7 @@ KF_HD void bfly2(cpx<S>* v, const cpx<S>* w) {
 
 // kf_bfly4, kiss_fft.c:38-84
 template <typename S, int VS>
-KF_HD void bfly4(cpx<S>* v, const cpx<S>* w, bool inverse) {
+KF_HD void bfly4(cpx<S>* v, const typename Ar<S>::CW* w, bool inverse) {
     typedef Ar<S> A;
     typedef typename A::CW CW;
     CW a0 = A::template fixdiv_w<4>(A::widen(v[0])), a1 = A::template fixdiv_w<4>(A::widen(v[VS]));
@@ -395,7 +397,7 @@ KF_HD void bfly4(cpx<S>* v, const cpx<S>* w, bool inverse) {
 // kf_bfly3, kiss_fft.c:86-128 (c0 = epi3 = tw[fstride*m]).  HALF_OF and
 // C_MULBYSCALAR act on the stored (truncated) sums.
 template <typename S, int VS>
-KF_HD void bfly3(cpx<S>* v, const cpx<S>* w, cpx<S> c0) {
+KF_HD void bfly3(cpx<S>* v, const typename Ar<S>::CW* w, typename Ar<S>::CW c0) {
     typedef Ar<S> A;
     typedef typename A::CW CW;
     typedef typename A::W W;
@@ -421,7 +423,7 @@ KF_HD void bfly3(cpx<S>* v, const cpx<S>* w, cpx<S> c0) {
 // kf_bfly5, kiss_fft.c:130-189 (c0 = ya = tw[fstride*m], c1 = yb = tw[2*fstride*m]).
 // S_MUL acts on the stored (truncated) sums and differences.
 template <typename S, int VS>
-KF_HD void bfly5(cpx<S>* v, const cpx<S>* w, cpx<S> ya, cpx<S> yb) {
+KF_HD void bfly5(cpx<S>* v, const typename Ar<S>::CW* w, typename Ar<S>::CW ya, typename Ar<S>::CW yb) {
     typedef Ar<S> A;
     typedef typename A::CW CW;
     typedef typename A::W W;
@@ -452,7 +454,8 @@ KF_HD void bfly5(cpx<S>* v, const cpx<S>* w, cpx<S> ya, cpx<S> yb) {
 }
 
 template <typename S, int P, int VS>
-KF_HD void bfly(cpx<S>* v, const cpx<S>* w, cpx<S> c0, cpx<S> c1, bool inverse) {
+KF_HD void bfly(cpx<S>* v, const typename Ar<S>::CW* w, typename Ar<S>::CW c0, typename Ar<S>::CW c1,
+                bool inverse) {
     if constexpr (P == 2) bfly2<S, VS>(v, w);
     if constexpr (P == 3) bfly3<S, VS>(v, w, c0);
     if constexpr (P == 4) bfly4<S, VS>(v, w, inverse);

@@ -276,12 +276,17 @@ KF_HD GroupIx decode(const KPass& ps, const KTab& tb, int J, int logJ, int col, 
     return g;
 }
 
+// The twiddles of butterfly u of a radix-P stage and the stage's constants,
+// as Ar<S>::CW (the compact table's entries; Q15 tables hold them widened).
 template <typename S, int P>
-KF_HD void stage_tw(const KTab& tb, const KStage& st, int u, cpx<S>* w, cpx<S>& c0, cpx<S>& c1) {
+KF_HD void stage_tw(const KTab& tb, const KStage& st, int u, typename Ar<S>::CW* w, typename Ar<S>::CW& c0,
+                    typename Ar<S>::CW& c1) {
+    typedef typename Ar<S>::CW CW;
+    typedef typename Ar<S>::W Wt;
     constexpr int W = P == 2 ? 1 : (P == 3 ? 2 : 4);
-    const cpx<S>* tws = (const cpx<S>*)tb.tw_stage + st.tw_off;
-    cpx<S> v[W];
-    ldro_vec<S, W>(tws + u * W, v);
+    const CW* tws = (const CW*)((const cpx<S>*)tb.tw_stage + st.tw_off);
+    CW v[W];
+    ldro_vec<Wt, W>(tws + u * W, v);
 #pragma unroll
     for (int q = 1; q < P; ++q) w[q - 1] = v[q - 1];
     if constexpr (P == 3 || P == 5) c0 = KF_LDG(tws + W * st.m);
@@ -304,7 +309,7 @@ KF_HD void group1(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
 #pragma unroll
         for (int q = 0; q < P; ++q) x[q] = t.sld(g.A0 + q * sa.iloc, g.job);
     }
-    C w[P > 1 ? P - 1 : 1], c0, c1;
+    typename Ar<S>::CW w[P > 1 ? P - 1 : 1], c0, c1;
     stage_tw<S, P>(tb, sa, g.ul * sb.m_low + U, w, c0, c1);
     bfly<S, P, 1>(x, w, c0, c1, sb.inverse != 0);
     if (dst_g) {
@@ -339,14 +344,14 @@ KF_HD void group2(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
             for (int ea = 0; ea < PA; ++ea) x[ea + PA * eb] = t.sld(g.A0 + ea * sa.iloc + eb * sbb.iloc, g.job);
     }
     {
-        C w[PB - 1], c0, c1;
+        typename Ar<S>::CW w[PB - 1], c0, c1;
         stage_tw<S, PB>(tb, sbb, g.ul * sb.m_low + U, w, c0, c1);
 #pragma unroll
         for (int ea = 0; ea < PA; ++ea) bfly<S, PB, PA>(x + ea, w, c0, c1, sb.inverse != 0);
     }
 #pragma unroll
     for (int eb = 0; eb < PB; ++eb) {
-        C w[PA - 1], c0, c1;
+        typename Ar<S>::CW w[PA - 1], c0, c1;
         stage_tw<S, PA>(tb, sa, (eb * sbb.mloc + g.ul) * sb.m_low + U, w, c0, c1);
         bfly<S, PA, 1>(x + PA * eb, w, c0, c1, sb.inverse != 0);
     }
@@ -395,14 +400,14 @@ KF_HD void group3(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
                     x[ea + PA * (eb + PB * ec)] = t.sld(g.A0 + ea * sa.iloc + eb * sbb.iloc + ec * sc.iloc, g.job);
     }
     {
-        C w[PC - 1], c0, c1;
+        typename Ar<S>::CW w[PC - 1], c0, c1;
         stage_tw<S, PC>(tb, sc, g.ul * sb.m_low + U, w, c0, c1);
 #pragma unroll
         for (int k = 0; k < PA * PB; ++k) bfly<S, PC, PA * PB>(x + k, w, c0, c1, sb.inverse != 0);
     }
 #pragma unroll
     for (int ec = 0; ec < PC; ++ec) {
-        C w[PB - 1], c0, c1;
+        typename Ar<S>::CW w[PB - 1], c0, c1;
         stage_tw<S, PB>(tb, sbb, (ec * sc.mloc + g.ul) * sb.m_low + U, w, c0, c1);
 #pragma unroll
         for (int ea = 0; ea < PA; ++ea) bfly<S, PB, PA>(x + ea + PA * PB * ec, w, c0, c1, sb.inverse != 0);
@@ -411,7 +416,7 @@ KF_HD void group3(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     for (int ec = 0; ec < PC; ++ec)
 #pragma unroll
         for (int eb = 0; eb < PB; ++eb) {
-            C w[PA - 1], c0, c1;
+            typename Ar<S>::CW w[PA - 1], c0, c1;
             stage_tw<S, PA>(tb, sa, (eb * sbb.mloc + ec * sc.mloc + g.ul) * sb.m_low + U, w, c0, c1);
             bfly<S, PA, 1>(x + PA * (eb + PB * ec), w, c0, c1, sb.inverse != 0);
         }
@@ -473,7 +478,7 @@ KF_HD void groupg(const Tile<S>& t, const KSub& sb, const KTab& tb, const KPass&
     if constexpr (kFixed) {
         typedef typename Arr::W W;
         constexpr int RP = gen_row(P);
-        // twiddles as W pairs (Q15 rows are pre-widened, kf_shape.h gen_units)
+        // twiddles as W pairs (Q15 rows are pre-widened, kf_shape.h tw_units)
         const CW* row = (const CW*)((const C*)tb.tw_stage + sa.tw_off) + (long long)u * P * RP;
 #if defined(__CUDA_ARCH__)
         // Q31: doubled legs for Ar::gen_out_q31

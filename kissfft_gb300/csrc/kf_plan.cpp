@@ -91,6 +91,20 @@ int max_tile_len(int dtype) { return tile_len_max(dtype); }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Twiddle slot `slot` of a compact stage table at base: a copy of the full
+// table's entry idx, or for Q15 that entry as a sign-extended int32 pair
+// (kf_shape.h tw_units)
+static void put_tw(int dtype, uint8_t* base, size_t slot, const uint8_t* full, size_t idx) {
+    const int esz = cpx_size(dtype);
+    if (dtype == KF_Q15) {
+        const int16_t* w = (const int16_t*)(full + idx * esz);
+        const int32_t pair[2] = {w[0], w[1]};
+        memcpy(base + slot * 8, pair, 8);
+    } else {
+        memcpy(base + slot * esz, full + idx * esz, esz);
+    }
+}
+
 bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
     dtype = dtype_;
     n = n_;
@@ -136,15 +150,7 @@ bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
                     long long idx = 0;
                     for (int q = 1; q < p; ++q) {
                         idx = (idx + step) % n;
-                        const size_t slot = (size_t)((u * p + q1) * RP + (q - 1));
-                        if (dtype == KF_Q15) {
-                            // sign-extended int32 pair (kf_shape.h gen_units)
-                            const int16_t* w = (const int16_t*)(twf.data() + (size_t)idx * esz);
-                            const int32_t pair[2] = {w[0], w[1]};
-                            memcpy(base + slot * 8, pair, 8);
-                        } else {
-                            memcpy(base + slot * esz, twf.data() + (size_t)idx * esz, esz);
-                        }
+                        put_tw(dtype, base, (size_t)((u * p + q1) * RP + (q - 1)), twf.data(), (size_t)idx);
                     }
                 }
             continue;
@@ -152,11 +158,10 @@ bool Plan::build(int dtype_, int n_, int inverse_, int lmax, int real_nfft_) {
         const int W = tw_width(p);
         uint8_t* base = tws.data() + (size_t)si.twoff[j] * esz;
         for (int u = 0; u < si.m[j]; ++u)
-            for (int q = 1; q < p; ++q)
-                memcpy(base + ((size_t)u * W + (q - 1)) * esz, twf.data() + (size_t)q * u * si.fs[j] * esz, esz);
-        uint8_t* cst = base + (size_t)W * si.m[j] * esz;
-        memcpy(cst, twf.data() + ((size_t)si.fs[j] * si.m[j] % n) * esz, esz);
-        memcpy(cst + esz, twf.data() + ((size_t)2 * si.fs[j] * si.m[j] % n) * esz, esz);
+            for (int q = 1; q < p; ++q) put_tw(dtype, base, (size_t)u * W + (q - 1), twf.data(), (size_t)q * u * si.fs[j]);
+        const size_t cst = (size_t)W * si.m[j];
+        put_tw(dtype, base, cst, twf.data(), (size_t)si.fs[j] * si.m[j] % n);
+        put_tw(dtype, base, cst + 1, twf.data(), (size_t)2 * si.fs[j] * si.m[j] % n);
     }
     // digit-reversal tables at the offsets make_shape assigned
     std::vector<int> rev((size_t)std::max(si.rev_total, 1), 0);

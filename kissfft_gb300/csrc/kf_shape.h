@@ -38,7 +38,11 @@ KF_CX int tile_len_max(int dtype) { return (128 * 1024) / cpx_bytes(dtype); }
 // u < m, tw_width(p) consecutive entries tw[q*u*fstride] (q = 1..p-1, then
 // padding), so one butterfly's twiddles are one or two vector loads; the
 // radix-3/5 constants (tw[fstride*m], tw[2*fstride*m]) follow the m rows.
+// Q15 tables (these and the generic rows below) hold every twiddle as a pair
+// of int32, the 16-bit values sign-extended, so the multiplies take them as
+// they are: tw_units(dtype) table entries per twiddle.
 KF_CX int tw_width(int p) { return p == 2 ? 1 : (p == 3 ? 2 : 4); }
+KF_CX int tw_units(int dtype) { return dtype == KF_Q15 ? 2 : 1; }
 
 KF_CX bool small_prime(int p) {
     return p == 7 || p == 11 || p == 13 || p == 17 || p == 19 || p == 23 || p == 29 || p == 31;
@@ -47,12 +51,8 @@ KF_CX bool small_prime(int p) {
 // Fixed-point generic-radix stages (p = 7..31) read their twiddles from
 // rows: for every u < m and output leg q1 < p, gen_row(p) consecutive
 // entries tw[(q*fstride*(u + q1*m)) mod N] for q = 1..p-1 (then padding) --
-// the exact sequence kf_bfly_generic walks (kiss_fft.c:218-226).  Q15 rows
-// hold each twiddle as a pair of int32 (the 16-bit values sign-extended, so
-// the multiplies take them as they are): gen_units(dtype) table entries
-// per twiddle.
+// the exact sequence kf_bfly_generic walks (kiss_fft.c:218-226).
 KF_CX int gen_row(int p) { return (p - 1 + 3) & ~3; }
-KF_CX int gen_units(int dtype) { return dtype == KF_Q15 ? 2 : 1; }
 
 // magic multiplier M with n / d == (n * M) >> 40 for n * d < 2^40
 KF_CX unsigned long long div_magic(int d) {
@@ -191,11 +191,11 @@ KF_CX ShapeInfo make_shape(int dtype, int n, int inverse, int lmax, int real_nff
         if (f[j] >= 2 && f[j] <= 5) {
             cnt = (cnt + 3) & ~3LL;  // 4-entry alignment for vector loads
             si.twoff[j] = (int)cnt;
-            cnt += (long long)tw_width(f[j]) * si.m[j] + 2;
+            cnt += ((long long)tw_width(f[j]) * si.m[j] + 2) * tw_units(dtype);
         } else if ((dtype == KF_Q15 || dtype == KF_Q31) && small_prime(f[j])) {
             cnt = (cnt + 3) & ~3LL;
             si.twoff[j] = (int)cnt;
-            cnt += (long long)gen_row(f[j]) * f[j] * si.m[j] * gen_units(dtype);
+            cnt += (long long)gen_row(f[j]) * f[j] * si.m[j] * tw_units(dtype);
         } else {
             si.twoff[j] = -1;
         }
