@@ -1094,11 +1094,12 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
             for (int tma = 1; tma >= 0; --tma) {
                 Step x = c;
                 x.tma_ok = tma;
+                const Step untimed = x;  // time_step adds the staging buffer to x's shared memory
                 float ms = time_step(x, roles, strm, e0, e1, 3);
                 if (ms > 0 && (bt < 0 || ms < bt)) {
                     bt = ms;
                     bc = {c.cfg.J, c.cfg.minb, tma, c.args.col_in, c.cfg.T, c.args.swz};
-                    bstep = x;
+                    bstep = untimed;
                 }
                 if (!x.args.tma) break;  // staging not eligible: one timing is enough
             }
