@@ -442,8 +442,8 @@ def run_mix(args, count=MIX_COUNT):
             L.kfg_batch_free(B)
     B, _, target = best
     t_commit = time.perf_counter() - t_commit
-    info = (ctypes.c_longlong * 4)()
-    L.kfg_batch_info(B, info, 4)
+    info = (ctypes.c_longlong * 5)()
+    L.kfg_batch_info(B, info, 5)
     direct_ms = timed(lambda: L.kfg_batch_run(B, st), max(3, args.steps // 3))
     if L.kfg_batch_capture(B, st) != 0:
         raise RuntimeError(L.kfg_last_error().decode())
@@ -467,10 +467,18 @@ def run_mix(args, count=MIX_COUNT):
     L.kfg_batch_free(B)
     single = percall_single(L, st)
     distinct = len(set((r[0], r[1], r[2]) for r in reqs))
+    peak, _ = peaks()
+    # the mix's own ceiling: compulsory bytes plus the intermediate round
+    # trip of every request longer than one shared tile (written, read back)
+    ceil_bytes = alg + int(info[4])
     return {"workload": "uneven mix: %d requests, nfft log-uniform [16, 131072], 80%% 2^a3^b5^c / 20%% with a "
                         "prime 7..31; 60%% c2c f32, 30%% r2c f32, 10%% c2c Q15; seed 3" % count,
             "requests": count, "distinct_plans": distinct, "compulsory_bytes": alg,
-            "graph": {"ms": round(graph_ms, 3), "gbs": round(alg / graph_ms / 1e6, 1)},
+            "intermediate_bytes": int(info[4]),
+            "graph": {"ms": round(graph_ms, 3), "gbs": round(alg / graph_ms / 1e6, 1),
+                      "frac_compulsory": round(alg / graph_ms / 1e6 / peak, 3),
+                      "hbm_gbs_with_intermediates": round(ceil_bytes / graph_ms / 1e6, 1),
+                      "frac_of_own_ceiling": round(ceil_bytes / graph_ms / 1e6 / peak, 3)},
             "direct": {"ms": round(direct_ms, 3), "gbs": round(alg / direct_ms / 1e6, 1)},
             "percall": {"ms": round(percall_ms, 3), "gbs": round(alg / percall_ms / 1e6, 1),
                         "us_per_request": round(percall_ms * 1e3 / count, 2)},
@@ -547,7 +555,9 @@ def run_configs(args):
     complex array; kiss_fftndr / kiss_fftndri on a 128^3 real array (every
     plan autotuned and its specialised kernels compiled first).  GB/s of
     compulsory bytes (c2c 2*N*8, r2c 4N + 8(N/2+1), nd 2*prod*8, ndr
-    4*prod + 8*prod/N*(N/2+1) per transform)."""
+    4*prod + 8*prod/N*(N/2+1) per transform).  Each row also carries
+    `graph`: ten of the same calls captured in one CUDA graph and replayed,
+    the device time without the per-call host work and launch gaps."""
     import torch
 
     import inputs
@@ -571,9 +581,29 @@ def run_configs(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    def row(byts, ms, note):
-        return {"ms": round(ms, 4), "gbs": round(byts / ms / 1e6, 1), "frac_of_measured_peak": round(byts / ms / 1e6 / peak, 3),
-                "note": note}
+    def graph_timed(fn, calls=10):
+        # the same calls captured once in a CUDA graph and replayed: device
+        # time without the host's per-call work and launch gaps
+        g = torch.cuda.CUDAGraph()
+        cs = torch.cuda.Stream()
+        cs.wait_stream(stream)
+        with torch.cuda.graph(g, stream=cs, capture_error_mode="thread_local"):
+            for _ in range(calls):
+                fn()
+        stream.wait_stream(cs)
+        g.replay()
+        ms = timed(g.replay) / calls
+        del g
+        return ms
+
+    def row(byts, ms, note, fn=None):
+        r = {"ms": round(ms, 4), "gbs": round(byts / ms / 1e6, 1), "frac_of_measured_peak": round(byts / ms / 1e6 / peak, 3),
+             "note": note}
+        if fn is not None:
+            gms = graph_timed(fn)
+            r["graph"] = {"ms": round(gms, 4), "gbs": round(byts / gms / 1e6, 1),
+                          "frac_of_measured_peak": round(byts / gms / 1e6 / peak, 3)}
+        return r
 
     out = {}
     # config 1: complex 1024 forward then inverse, 4096 transforms
@@ -584,8 +614,8 @@ def run_configs(args):
     for c in (fw, iv):
         kf.autotune(c, 4096)
         kf.prepare(c, 4096)
-    ms = timed(lambda: (kf.kiss_fft_batch(fw, x, y, 4096), kf.kiss_fft_batch(iv, y, z, 4096)))
-    out["c2c_1024_fwd_inv_4096"] = row(2 * 2 * 1024 * 8 * 4096, ms, "32 MiB each way: L2-resident")
+    fn = lambda: (kf.kiss_fft_batch(fw, x, y, 4096), kf.kiss_fft_batch(iv, y, z, 4096))  # noqa: E731
+    out["c2c_1024_fwd_inv_4096"] = row(2 * 2 * 1024 * 8 * 4096, timed(fn), "32 MiB each way: L2-resident", fn)
     del x, y, z
     # config 3: real 4096 x 65536 (1 GiB of reals)
     B, N = 65536, 4096
@@ -605,8 +635,10 @@ def run_configs(args):
         kf.autotune(c, B)
         kf.prepare(c, B)
     rbytes = (4 * N + 8 * (N // 2 + 1)) * B
-    out["r2c_4096_65536"] = row(rbytes, timed(lambda: kf.kiss_fftr_batch(rf, tr, fr, B)), "1 GiB in")
-    out["c2r_4096_65536"] = row(rbytes, timed(lambda: kf.kiss_fftri_batch(ri, fr, back, B)), "1 GiB out")
+    fn = lambda: kf.kiss_fftr_batch(rf, tr, fr, B)  # noqa: E731
+    out["r2c_4096_65536"] = row(rbytes, timed(fn), "1 GiB in", fn)
+    fn = lambda: kf.kiss_fftri_batch(ri, fr, back, B)  # noqa: E731
+    out["c2r_4096_65536"] = row(rbytes, timed(fn), "1 GiB out", fn)
     del tr, fr, back
     # config 3: 2-D complex 2048^2 and real 128^3
     a = torch.from_numpy(inputs.cpx((2048, 2048), "float", 2).view(np.float32).copy()).to(dev)
@@ -614,7 +646,8 @@ def run_configs(args):
     nd = kf.kiss_fftnd_alloc([2048, 2048], 0)
     kf.autotune(nd, 1)
     kf.prepare(nd, 1)
-    out["nd_2048x2048"] = row(2 * 2048 * 2048 * 8, timed(lambda: kf.kiss_fftnd(nd, a, b)), "32 MiB: L2-resident")
+    fn = lambda: kf.kiss_fftnd(nd, a, b)  # noqa: E731
+    out["nd_2048x2048"] = row(2 * 2048 * 2048 * 8, timed(fn), "32 MiB: L2-resident", fn)
     rng = np.random.default_rng(2)
     v = torch.from_numpy(rng.standard_normal((128, 128, 128)).astype(np.float32)).to(dev)
     w = torch.empty((128, 128, 65, 2), device=dev, dtype=torch.float32)
@@ -624,8 +657,10 @@ def run_configs(args):
         kf.autotune(c, 1)
         kf.prepare(c, 1)
     nbytes = 4 * 128 ** 3 + 8 * 128 * 128 * 65
-    out["ndr_128^3"] = row(nbytes, timed(lambda: kf.kiss_fftndr(ndr, v, w)), "8 MiB: L2-resident")
-    out["ndri_128^3"] = row(nbytes, timed(lambda: kf.kiss_fftndri(ndri, w, v2)), "8 MiB: L2-resident")
+    fn = lambda: kf.kiss_fftndr(ndr, v, w)  # noqa: E731
+    out["ndr_128^3"] = row(nbytes, timed(fn), "8 MiB: L2-resident", fn)
+    fn = lambda: kf.kiss_fftndri(ndri, w, v2)  # noqa: E731
+    out["ndri_128^3"] = row(nbytes, timed(fn), "8 MiB: L2-resident", fn)
     return out
 
 

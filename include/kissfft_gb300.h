@@ -163,7 +163,9 @@ int kfg_batch_run(kfg_batch *b, void *stream);
 int kfg_batch_capture(kfg_batch *b, void *stream);
 /* the plain per-call form of the same work: one drop-in call per request */
 int kfg_batch_run_percall(kfg_batch *b, void *stream);
-/* out[0] requests, out[1] launch steps, out[2] kernel launches, out[3] tiles */
+/* out[0] requests, out[1] launch steps, out[2] kernel launches, out[3] tiles,
+ * out[4] bytes of intermediate traffic: requests longer than one shared tile
+ * write their intermediate results to device scratch and read them back */
 int kfg_batch_info(const kfg_batch *b, long long *out, int nout);
 void kfg_batch_free(kfg_batch *b);
 

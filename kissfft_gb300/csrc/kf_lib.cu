@@ -1274,6 +1274,7 @@ struct kfg_batch {
     std::vector<Launch> launches;
     std::vector<void*> allocs;
     std::vector<kfg_plan*> req_plan;
+    long long scratch_bytes = 0;  // intermediates of multi-pass requests (each written once, read once)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
 
@@ -1289,6 +1290,7 @@ struct kfg_batch {
         launches.clear();
         steps.clear();
         d_steps = nullptr;
+        scratch_bytes = 0;
         committed = false;
     }
     ~kfg_batch() {
@@ -1350,6 +1352,7 @@ int batch_commit(kfg_batch* b) {
         long long* d_oo = upload(b, oo);
         void* scr = nullptr;
         const size_t off1 = (s.scratch[0] + 255) & ~(size_t)255;
+        b->scratch_bytes += (long long)(s.scratch[0] + s.scratch[1]);
         if (s.scratch[0] + s.scratch[1] > 0) {
             if (cudaMalloc(&scr, off1 + s.scratch[1]) != cudaSuccess) return fail(KFG_ENOMEM, "kfg_batch: scratch");
             b->allocs.push_back(scr);
@@ -1592,8 +1595,9 @@ int kfg_batch_info(const kfg_batch* b, long long* out, int nout) {
     if (!b || !out) return KFG_EINVAL;
     long long items = 0;
     for (auto& L : b->launches) items += (long long)L.items.size();
-    long long v[4] = {(long long)b->reqs.size(), (long long)b->steps.size(), (long long)b->launches.size(), items};
-    for (int i = 0; i < nout && i < 4; ++i) out[i] = v[i];
+    long long v[5] = {(long long)b->reqs.size(), (long long)b->steps.size(), (long long)b->launches.size(), items,
+                      2 * b->scratch_bytes};
+    for (int i = 0; i < nout && i < 5; ++i) out[i] = v[i];
     return KFG_OK;
 }
 

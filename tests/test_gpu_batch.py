@@ -175,8 +175,23 @@ def test_batch_info_and_errors(core):
         import torch
         a = torch.zeros(4096, dtype=torch.uint8, device="cuda")
         assert L.kfg_batch_commit(B, vp(a.data_ptr()), vp(a.data_ptr() + 2048 * 0), 0) == 0
-        info = (ctypes.c_longlong * 4)()
-        assert L.kfg_batch_info(B, info, 4) == 0
+        info = (ctypes.c_longlong * 5)()
+        assert L.kfg_batch_info(B, info, 5) == 0
         assert info[0] == 5 and info[2] >= 1 and info[3] >= 1
+        assert info[4] == 0  # 64-point requests fit one shared tile: no intermediate traffic
+    finally:
+        L.kfg_batch_free(B)
+    # one 65536-point float request runs two passes through an intermediate
+    # of 65536 complex floats: written once, read once
+    B = L.kfg_batch_create()
+    try:
+        n = 65536
+        assert L.kfg_batch_add(B, 1, 0, n, 0, 0) == 0
+        a = torch.zeros(n * 8, dtype=torch.uint8, device="cuda")
+        c = torch.zeros(n * 8, dtype=torch.uint8, device="cuda")
+        assert L.kfg_batch_commit(B, vp(a.data_ptr()), vp(c.data_ptr()), 0) == 0
+        info = (ctypes.c_longlong * 5)()
+        assert L.kfg_batch_info(B, info, 5) == 0
+        assert info[4] == 2 * n * 8
     finally:
         L.kfg_batch_free(B)
