@@ -6,6 +6,17 @@
 
 namespace kf {
 
+// ------------------------------------------------- programmatic dependent launch
+// Engine launches may start while the previous kernel in their stream
+// finishes (launch attribute programmaticStreamSerialization): every block
+// first waits until that kernel has completed and its writes are visible
+// (a no-op for a launch without the attribute), then lets the next launch
+// in the stream begin to launch.  No global memory is touched before the wait.
+__device__ __forceinline__ void kf_pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- TMA staging
 // One-dimensional bulk copies global -> shared completing on an mbarrier
 // (cp.async.bulk, sm_90+).  Every wait is bounded: past the limit the kernel
@@ -96,6 +107,7 @@ struct DevExec {
 // compile time (specialised kernels); 0 takes it from the arguments.
 template <typename S, int MODE, kmask_t KM, int JF = 0, int CIF = -1, int COF = -1, int SWF = -1>
 __device__ __forceinline__ void engine_body(const KRun& a, const KSub& s0, const KSub& s1) {
+    kf_pdl_enter();
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
     __shared__ int s_U[KF_MAXJ];
@@ -128,6 +140,7 @@ __device__ __forceinline__ void engine_body(const KRun& a, const KSub& s0, const
 // passes; the first pass reads the staged tile through shared memory.
 template <typename S, int MODE, kmask_t KM, int JF = 0, int SWF = -1>
 __device__ __forceinline__ void engine_body_tma(const KRun& a, const KSub& s0) {
+    kf_pdl_enter();
     extern __shared__ __align__(16) unsigned char kf_dyn_smem[];
     __shared__ long long s_inb[KF_MAXJ], s_outb[KF_MAXJ], s_lin[KF_MAXJ], s_lout[KF_MAXJ];
     __shared__ int s_U[KF_MAXJ];

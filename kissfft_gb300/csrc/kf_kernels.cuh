@@ -7,6 +7,7 @@
 #include "kf_plan.h"
 
 #include <atomic>
+#include <cstdlib>
 #include <string>
 
 namespace kf {
@@ -50,6 +51,32 @@ inline long long launch_grid(const void* k, const Step& st) {
     return grid;
 }
 
+// Engine launches carry the programmatic-stream-serialization attribute
+// (the kernels wait for the previous kernel on entry, kf_pdl_enter), so the
+// next launch of a schedule overlaps the tail of the one before it.
+// KISSFFT_GB300_PDL=0 launches them plainly.
+inline bool pdl_enabled() {
+    static const bool on = [] {
+        const char* e = getenv("KISSFFT_GB300_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+inline cudaError_t launch_engine_raw(const void* k, long long grid, const Step& st, void** args, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)st.cfg.T);
+    cfg.dynamicSmemBytes = (size_t)st.cfg.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelExC(&cfg, k, args);
+}
+
 template <typename S, int MODE, int FAM>
 static cudaError_t launch_engine_f(const Step& st, cudaStream_t s) {
     auto k = kf_engine_kernel<S, MODE, FAM>;
@@ -62,8 +89,8 @@ static cudaError_t launch_engine_f(const Step& st, cudaStream_t s) {
     }
     const long long grid = launch_grid((const void*)k, st);
     if (grid <= 0) return cudaSuccess;
-    k<<<(unsigned)grid, st.cfg.T, st.cfg.smem, s>>>(st.args);
-    return cudaGetLastError();
+    void* args[] = {(void*)&st.args};
+    return launch_engine_raw((const void*)k, grid, st, args, s);
 }
 
 template <typename S>
@@ -140,7 +167,7 @@ inline cudaError_t launch_spec(const void* k, const Step& st, cudaStream_t s) {
     if (grid <= 0) return cudaSuccess;
     // the specialised kernels take the run-time part only (their shape is compiled in)
     void* args[] = {(void*)static_cast<const KRun*>(&st.args)};
-    return cudaLaunchKernel(k, dim3((unsigned)grid), dim3(st.cfg.T), args, (size_t)st.cfg.smem, s);
+    return launch_engine_raw(k, grid, st, args, s);
 }
 
 inline cudaError_t launch_step(const Step& st, cudaStream_t s) {

@@ -508,7 +508,7 @@ std::string plan_sig(const kfg_plan* p) {
         snprintf(name, sizeof(name), "%s", prop.name);
     for (char* c = name; *c; ++c)
         if (*c == ' ') *c = '_';
-    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v5";
+    o << ":" << name << ":spec" << (specialize_enabled() ? 1 : 0) << ":v6";
     return o.str();
 }
 
@@ -1029,16 +1029,26 @@ int kfg_autotune(kfg_plan* p, long long batch, long long in_dist, long long out_
     cudaStreamCreate(&strm);
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    int nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     for (auto& st0 : s.steps) {
         if (st0.kind != 0) continue;
         std::vector<Step> cands;
         const int J0 = st0.cfg.J;
+        // a launch with few tiles for the SMs (small batches, N-D axes) runs
+        // about one wave, as long as one tile's latency: narrower tiles too
+        const bool few_tiles = (st0.args.G + J0 - 1) / J0 < 4LL * std::max(nsm, 1);
         // row-mode steps also try column-layout tiles with 2..8 jobs
         Step colst = st0;
         const bool can_col = recolumn_step(colst);
         for (int col = 0; col <= (can_col ? 1 : 0); ++col) {
             const Step& base = col ? colst : st0;
-            const std::vector<int> Js = col ? std::vector<int>{2, 4, 8} : std::vector<int>{J0 / 2, J0, J0 * 2, J0 * 4};
+            std::vector<int> Js = col ? std::vector<int>{2, 4, 8} : std::vector<int>{J0 / 2, J0, J0 * 2, J0 * 4};
+            if (few_tiles && !col) {
+                Js.push_back(J0 / 4);
+                Js.push_back(J0 / 8);
+            }
             for (int J : Js) {
                 Step c = base;
                 if (J < 1 || (J != base.cfg.J && !reshape_step(c, J))) continue;
