@@ -546,6 +546,48 @@ def run_serve_burst(args):
 
 
 # ------------------------------------------------------------------ other configs
+def _configs_1d(args, kf, inputs, dev, timed, row):
+    """Config 1 (1024-point forward + inverse on 4096 transforms) and config
+    3's real 4096 x 65536 pair, for run_configs."""
+    import torch
+
+    out = {}
+    x = torch.from_numpy(inputs.cpx((4096, 1024), "float", 0).view(np.float32).copy()).to(dev)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    fw, iv = kf.kiss_fft_alloc(1024, 0), kf.kiss_fft_alloc(1024, 1)
+    for c in (fw, iv):
+        kf.autotune(c, 4096)
+        kf.prepare(c, 4096)
+    fn = lambda: (kf.kiss_fft_batch(fw, x, y, 4096), kf.kiss_fft_batch(iv, y, z, 4096))  # noqa: E731
+    out["c2c_1024_fwd_inv_4096"] = row(2 * 2 * 1024 * 8 * 4096, timed(fn), "32 MiB each way: L2-resident", fn)
+    del x, y, z
+    # config 3: real 4096 x 65536 (1 GiB of reals)
+    B, N = 65536, 4096
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    t = torch.arange(N, device=dev, dtype=torch.float32)
+    tr = torch.empty((B, N), device=dev, dtype=torch.float32)
+    for r0 in range(0, B, 8192):
+        f = torch.rand((8192, 3, 1), device=dev, generator=g) * (N / 2)
+        ph = torch.rand((8192, 3, 1), device=dev, generator=g) * 6.283185307179586
+        tr[r0:r0 + 8192] = torch.cos(6.283185307179586 * f * t / N + ph).sum(1) + \
+            0.1 * torch.randn((8192, N), device=dev, generator=g)
+    fr = torch.empty((B, N // 2 + 1, 2), device=dev, dtype=torch.float32)
+    back = torch.empty_like(tr)
+    rf, ri = kf.kiss_fftr_alloc(N, 0), kf.kiss_fftr_alloc(N, 1)
+    for c in (rf, ri):
+        kf.autotune(c, B)
+        kf.prepare(c, B)
+    rbytes = (4 * N + 8 * (N // 2 + 1)) * B
+    fn = lambda: kf.kiss_fftr_batch(rf, tr, fr, B)  # noqa: E731
+    out["r2c_4096_65536"] = row(rbytes, timed(fn), "1 GiB in", fn)
+    fn = lambda: kf.kiss_fftri_batch(ri, fr, back, B)  # noqa: E731
+    out["c2r_4096_65536"] = row(rbytes, timed(fn), "1 GiB out", fn)
+    del tr, fr, back
+    return out
+
+
 def run_configs(args):
     """The reference's other workloads, each timed alone (back-to-back
     launches between two events, after a warm launch): the 1024-point
@@ -606,40 +648,9 @@ def run_configs(args):
         return r
 
     out = {}
-    # config 1: complex 1024 forward then inverse, 4096 transforms
-    x = torch.from_numpy(inputs.cpx((4096, 1024), "float", 0).view(np.float32).copy()).to(dev)
-    y = torch.empty_like(x)
-    z = torch.empty_like(x)
-    fw, iv = kf.kiss_fft_alloc(1024, 0), kf.kiss_fft_alloc(1024, 1)
-    for c in (fw, iv):
-        kf.autotune(c, 4096)
-        kf.prepare(c, 4096)
-    fn = lambda: (kf.kiss_fft_batch(fw, x, y, 4096), kf.kiss_fft_batch(iv, y, z, 4096))  # noqa: E731
-    out["c2c_1024_fwd_inv_4096"] = row(2 * 2 * 1024 * 8 * 4096, timed(fn), "32 MiB each way: L2-resident", fn)
-    del x, y, z
-    # config 3: real 4096 x 65536 (1 GiB of reals)
-    B, N = 65536, 4096
-    g = torch.Generator(device=dev)
-    g.manual_seed(2)
-    t = torch.arange(N, device=dev, dtype=torch.float32)
-    tr = torch.empty((B, N), device=dev, dtype=torch.float32)
-    for r0 in range(0, B, 8192):
-        f = torch.rand((8192, 3, 1), device=dev, generator=g) * (N / 2)
-        ph = torch.rand((8192, 3, 1), device=dev, generator=g) * 6.283185307179586
-        tr[r0:r0 + 8192] = torch.cos(6.283185307179586 * f * t / N + ph).sum(1) + \
-            0.1 * torch.randn((8192, N), device=dev, generator=g)
-    fr = torch.empty((B, N // 2 + 1, 2), device=dev, dtype=torch.float32)
-    back = torch.empty_like(tr)
-    rf, ri = kf.kiss_fftr_alloc(N, 0), kf.kiss_fftr_alloc(N, 1)
-    for c in (rf, ri):
-        kf.autotune(c, B)
-        kf.prepare(c, B)
-    rbytes = (4 * N + 8 * (N // 2 + 1)) * B
-    fn = lambda: kf.kiss_fftr_batch(rf, tr, fr, B)  # noqa: E731
-    out["r2c_4096_65536"] = row(rbytes, timed(fn), "1 GiB in", fn)
-    fn = lambda: kf.kiss_fftri_batch(ri, fr, back, B)  # noqa: E731
-    out["c2r_4096_65536"] = row(rbytes, timed(fn), "1 GiB out", fn)
-    del tr, fr, back
+    nd_only = args.only == "nd"  # the N-D workloads alone (small: 32 MiB and 8 MiB arrays)
+    if not nd_only:
+        out.update(_configs_1d(args, kf, inputs, dev, timed, row))
     # config 3: 2-D complex 2048^2 and real 128^3
     a = torch.from_numpy(inputs.cpx((2048, 2048), "float", 2).view(np.float32).copy()).to(dev)
     b = torch.empty_like(a)
@@ -876,8 +887,9 @@ def main():
     ap.add_argument("--serve-hold", type=float, default=60.0,
                     help="seconds the serving loop is held at 50,000 requests/s")
     ap.add_argument("--no-configs", action="store_true", help="skip the real / N-D / round-trip workloads")
-    ap.add_argument("--only", choices=["mix", "serve", "configs", "mix-runs", "serve-burst"], default=None,
-                    help="run only the uneven-mix or the serving measurement and print it")
+    ap.add_argument("--only", choices=["mix", "serve", "configs", "nd", "mix-runs", "serve-burst"], default=None,
+                    help="run only one measurement and print it: the uneven mix, serving, the other workloads "
+                         "(configs) or their N-D part (nd), the mix's launch runs, a serving burst")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch of the dominant kernel from an ncu capture")
     ap.add_argument("--specialize", type=int, default=1,
@@ -938,7 +950,7 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(0)
-        fn = {"mix": run_mix, "serve": run_serving, "configs": run_configs, "mix-runs": run_mix_runs,
+        fn = {"mix": run_mix, "serve": run_serving, "configs": run_configs, "nd": run_configs, "mix-runs": run_mix_runs,
               "serve-burst": run_serve_burst}[args.only]
         print(json.dumps(fn(args)))
         return
