@@ -69,7 +69,7 @@ inline cudaError_t launch_engine_raw(const void* k, long long grid, const Step& 
     cfg.blockDim = dim3((unsigned)st.cfg.T);
     cfg.dynamicSmemBytes = (size_t)st.cfg.smem;
     cfg.stream = s;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[1] = {};
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
