@@ -545,10 +545,10 @@ def run_serve_burst(args):
     return r
 
 
-# ------------------------------------------------------------------ other configs
+# ------------------------------------------------------------------ other workloads
 def _configs_1d(args, kf, inputs, dev, timed, row):
-    """Config 1 (1024-point forward + inverse on 4096 transforms) and config
-    3's real 4096 x 65536 pair, for run_configs."""
+    """The 1024-point forward + inverse round trip on 4096 transforms and the
+    real 4096-point forward / inverse pair on 65536 rows, for run_configs."""
     import torch
 
     out = {}
@@ -562,7 +562,7 @@ def _configs_1d(args, kf, inputs, dev, timed, row):
     fn = lambda: (kf.kiss_fft_batch(fw, x, y, 4096), kf.kiss_fft_batch(iv, y, z, 4096))  # noqa: E731
     out["c2c_1024_fwd_inv_4096"] = row(2 * 2 * 1024 * 8 * 4096, timed(fn), "32 MiB each way: L2-resident", fn)
     del x, y, z
-    # config 3: real 4096 x 65536 (1 GiB of reals)
+    # real 4096-point rows x 65536 (1 GiB of reals)
     B, N = 65536, 4096
     g = torch.Generator(device=dev)
     g.manual_seed(2)
@@ -651,7 +651,7 @@ def run_configs(args):
     nd_only = args.only == "nd"  # the N-D workloads alone (small: 32 MiB and 8 MiB arrays)
     if not nd_only:
         out.update(_configs_1d(args, kf, inputs, dev, timed, row))
-    # config 3: 2-D complex 2048^2 and real 128^3
+    # 2-D complex 2048^2 and 3-D real 128^3
     a = torch.from_numpy(inputs.cpx((2048, 2048), "float", 2).view(np.float32).copy()).to(dev)
     b = torch.empty_like(a)
     nd = kf.kiss_fftnd_alloc([2048, 2048], 0)

@@ -353,7 +353,7 @@ def test_fastfir_streaming_matches_whole_signal(kf):
     assert np.allclose(got, whole, rtol=0, atol=1e-5)
 
 
-def test_round_trip_config1(kf):
+def test_round_trip_1024_on_4096(kf):
     """4096 x 1024-point complex float forward then inverse: N*x back."""
     import torch
     n, b = 1024, 4096
@@ -370,7 +370,7 @@ def test_round_trip_config1(kf):
 
 
 @pytest.mark.parametrize("dtype", ["int16_t", "int32_t"])
-def test_fixed_point_config2_batches(kf, dtype):
+def test_fixed_point_bench_batches(kf, dtype):
     """The mixed-radix sizes at larger batches, bit-exact against the oracle."""
     for n, b in [(480, 512), (1000, 256), (3003, 64), (65536, 8)]:
         x = inputs.cpx((b, n), dtype, 1)
@@ -382,7 +382,7 @@ def test_fixed_point_config2_batches(kf, dtype):
         assert np.array_equal(y, ref), (dtype, n)
 
 
-def test_real_config3_round_trip(kf):
+def test_real_4096_round_trip(kf):
     """kiss_fftr / kiss_fftri at 4096 on sinusoids plus noise: ri(r(x)) = N*x."""
     import torch
     n, b = 4096, 512
@@ -400,7 +400,7 @@ def test_real_config3_round_trip(kf):
     assert relerr_rows(r.astype(np.float64) / n, t.astype(np.float64)) <= 4 * bound("float", n)
 
 
-def test_nd_config3_sizes(kf):
+def test_nd_2048_square_and_128_cube(kf):
     """2048 x 2048 complex and 128^3 real N-D transforms against numpy."""
     x = inputs.cpx((2048, 2048), "float", 2)
     cfg = kf.kiss_fftnd_alloc([2048, 2048], 0)
