@@ -188,6 +188,36 @@ def test_forced_tile_shapes(emu):
             emu.emu_force(0, 0)
 
 
+@pytest.mark.parametrize("dtype", ["int16_t", "int32_t"])
+def test_narrow_tiles_real_and_nd(emu, dtype):
+    """Tiles of 1, 2 and 4 jobs (the narrower shapes the autotuner also times
+    for launches with few tiles per SM) on real rows, both directions, and
+    on every axis of N-D arrays, including the 128^3-style real-row shape:
+    bit-exact against the oracle."""
+    for J in (1, 2, 4):
+        emu.emu_force(J, 0)
+        try:
+            for nfft in (128, 480, 4096):
+                t = inputs.real((5, nfft), dtype, nfft + J)
+                f = kfo.empty_cpx((5, nfft // 2 + 1), dtype)
+                assert emu.emu_r2c(DT[dtype], nfft, 0, p(t), p(f), L(5)) == 0
+                assert np.array_equal(f, kfo.fftr(t, dtype)), (J, nfft)
+                g = inputs.cpx((5, nfft // 2 + 1), dtype, nfft + J + 1)
+                t2 = np.zeros((5, nfft), kfo.SCALAR[dtype])
+                assert emu.emu_c2r(DT[dtype], nfft, 0, p(g), p(t2), L(5)) == 0
+                assert np.array_equal(t2, kfo.fftri(g, nfft, dtype)), (J, nfft)
+            for dims in ([16, 65], [128, 6], [3, 64, 5]):
+                for inv in (0, 1):
+                    x = inputs.cpx(tuple(dims), dtype, 20 + J + inv)
+                    buf = x.copy()
+                    d = (ctypes.c_int * len(dims))(*dims)
+                    for ax in range(len(dims)):
+                        assert emu.emu_axis(DT[dtype], d, len(dims), ax, inv, p(buf)) == 0
+                    assert np.array_equal(buf, kfo.fftnd(x, dims, inv, dtype)), (J, dims, inv)
+        finally:
+            emu.emu_force(0, 0)
+
+
 @pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("dtype", ["int16_t", "int32_t", "float"])
 def test_shared_index_maps(emu, dtype, mode):
