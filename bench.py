@@ -59,10 +59,10 @@ DTYPES = ["float", "int16_t", "int32_t"]
 ESZ = {"float": 8, "double": 16, "int16_t": 4, "int32_t": 8}
 BATCH_BYTES = 256 * 1024 * 1024
 # DRAM bytes (read + write) per launch measured by ncu on these exact
-# launches (profiles/ncu_q15_3003_generic_radix.md, profiles/ncu_fixed_point_bench_sizes.md,
-# profiles/ncu_engine_kernels_bench_sizes.md); the write figure misses the
+# launches (profiles/ncu_q15_3003_generic_radix.md, profiles/ncu_dram_traffic_3003.md,
+# profiles/ncu_fixed_point_bench_sizes.md); the write figure misses the
 # dirty lines still in L2 when the capture ends
-NCU_TRAFFIC = {("int16_t", 3003, 22347): 485.3e6, ("int32_t", 3003, 11173): 483.2e6, ("float", 1000, 33554): 485.8e6,
+NCU_TRAFFIC = {("int16_t", 3003, 22347): 485.3e6, ("int32_t", 3003, 11173): 483.2e6,
                ("int16_t", 1000, 67108): 483.1e6, ("int32_t", 65536, 512): 486.7e6}
 
 
